@@ -1,0 +1,182 @@
+/*
+ * smat.h — C ABI of libsmat, a GB300 (sm_103a) implementation of the SMaT
+ * pipeline: Jaccard row reordering -> BCSR blocking -> block-sparse x dense
+ * SpMM on tcgen05 tensor cores.
+ *
+ * Conventions
+ *  - Every entry point returns an smat_status; smat_last_error() gives a
+ *    one-line message for the calling thread's last failure. Nothing here
+ *    calls exit().
+ *  - Host pointers are marked (host), device pointers (device).
+ *  - Device work is enqueued on the given stream (a cudaStream_t passed as
+ *    void*; NULL = legacy default stream) and is asynchronous.
+ *  - smat_spmm allocates nothing and synchronises nothing; scratch for the
+ *    forms that convert B is passed in by the caller.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths inside ajit283/sptc-smat).
+ */
+#ifndef SMAT_H_
+#define SMAT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum smat_status {
+  SMAT_OK = 0,
+  SMAT_ERR_INVALID = 1,     /* malformed argument or matrix */
+  SMAT_ERR_UNSUPPORTED = 2, /* option or shape not implemented */
+  SMAT_ERR_CUDA = 3,        /* CUDA runtime / driver error */
+  SMAT_ERR_NOMEM = 4,       /* host or device allocation failed */
+  SMAT_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired */
+  SMAT_ERR_NO_DEVICE = 6    /* no usable sm_103 device / kernels not loadable */
+} smat_status;
+
+typedef enum smat_dtype {
+  SMAT_F32 = 0,
+  SMAT_F16 = 1,
+  SMAT_BF16 = 2,
+  SMAT_F64 = 3,
+  SMAT_E4M3 = 4
+} smat_dtype;
+
+/* Arithmetic form of the SpMM. All forms accumulate in FP32 (TMEM). */
+typedef enum smat_form {
+  SMAT_FORM_F16 = 0,        /* FP16 A and B (the plain form) */
+  SMAT_FORM_BF16 = 1,       /* BF16 A and B */
+  SMAT_FORM_FP8 = 2,        /* e4m3 A with one FP32 scale per block */
+  SMAT_FORM_SPLIT_BF16 = 3  /* hi+lo BF16 A and B, three products */
+} smat_form;
+
+typedef enum smat_layout { SMAT_ROW_MAJOR = 0, SMAT_COL_MAJOR = 1 } smat_layout;
+
+/* A sparse matrix in CSR (host). Column indices within a row are kept in the
+ * given order ("file order"); values may be NULL (pattern: every value 1). */
+typedef struct smat_csr {
+  int64_t rows;
+  int64_t cols;
+  int64_t nnz;
+  const int64_t* row_ptr; /* (host) rows + 1 */
+  const int32_t* col_idx; /* (host) nnz */
+  const void* values;     /* (host) nnz elements of values_dtype, or NULL */
+  int32_t values_dtype;   /* SMAT_F32, SMAT_F16 or SMAT_F64 */
+} smat_csr;
+
+/* BCSR build options. */
+typedef struct smat_bcsr_opts {
+  int32_t block_rows;     /* bh: 16 (default when 0) */
+  int32_t block_cols;     /* bw: 16 (default when 0) */
+  uint32_t forms;         /* bit (1 << smat_form) per form to materialise; 0 = F16 only */
+  int32_t use_24;         /* 1: blocks that are exactly 2:4 use the sparse tensor-core path */
+  const int64_t* row_perm;/* (host, optional) new row r = old row row_perm[r]; SpMM results
+                             are written back in the ORIGINAL row order */
+  int32_t device;         /* CUDA device ordinal */
+  int32_t panel_rows;     /* block rows per tensor-core work item (0 = autotuned) */
+} smat_bcsr_opts;
+
+typedef struct smat_bcsr smat_bcsr; /* opaque handle, immutable after create */
+
+typedef struct smat_bcsr_info {
+  int64_t rows, cols;           /* logical (unpadded) shape */
+  int64_t rows_padded, cols_padded;
+  int64_t nnz;                  /* scalar nonzeros stored in the input CSR */
+  int64_t nnzb;                 /* nonzero blocks */
+  int64_t n_blocks_24;          /* blocks that are exactly 2:4 (0 unless use_24) */
+  int32_t block_rows, block_cols;
+  int32_t panel_rows;
+  int32_t n_panels;
+  int64_t n_union_cols;         /* B tiles one SpMM pass loads (per N tile) */
+  double fill;                  /* nnz / (nnzb * bh * bw) */
+} smat_bcsr_info;
+
+typedef struct smat_reorder_stats {
+  int64_t comparisons;          /* distance evaluations (blocking.cpp comparison_counter) */
+  int64_t merges;               /* rows merged under tau (merge_counter) */
+} smat_reorder_stats;
+
+/* ---------------------------------------------------------------- step 1 */
+
+/* Row reordering. Replaces `Matrix_Blocking -f x.el -a algo -b col_block
+ * -B row_block -F force_fixed -t tau` (preprocess/test/general/Matrix_Blocking.cpp:10-50,
+ * driven by src/reorder.py:131-132) and in-process
+ * BlockingEngine::GetGrouping + CSR::reorder (preprocess/src/general/blocking.cpp:616-657,
+ * csr.cpp:97-105). algo 5 (IterativeBlockingKeeper, the pipeline's choice)
+ * and 2 (fixed size) are supported. perm_out[r] = old row placed at new row r,
+ * identical to the reference's permutation; grouping_out (optional) receives
+ * the final grouping vector (the reference's ".g" file content). A column
+ * index is "the" column (col_idx); the pattern is used, values are ignored.
+ * On an sm_103 device the candidate scan runs on the GPU when use_gpu != 0. */
+smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
+                         int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
+                         int64_t* grouping_out, smat_reorder_stats* stats);
+
+/* ---------------------------------------------------------------- step 2 */
+
+/* CSR -> BCSR, uploaded to the device. Replaces the SparseMatrix constructor
+ * (src/cuda_hgemm/src/common/matrix.h:161-246: csrToBcsr :666-792 and
+ * filterBcsrBlocks :1140-1288). Rows are padded to a multiple of bh and
+ * columns to a multiple of bw (mmio_highlevel.h:514-520). The block structure
+ * and values are bit-identical to csrToBcsr on the (optionally permuted) CSR. */
+smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat_bcsr** out);
+smat_status smat_bcsr_destroy(smat_bcsr* A);
+smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info);
+
+/* Copy the block structure back to the host (for checking against the
+ * reference): row_ptr[rows_padded/bh + 1], col_idx[nnzb] (column START of
+ * each block, as bcsrColIdx in matrix.h:743), values[nnzb*bh*bw] as FP16 bit
+ * patterns, row-major inside each block. Any pointer may be NULL. */
+smat_status smat_bcsr_export(const smat_bcsr* A, int32_t* row_ptr, int32_t* col_idx,
+                             uint16_t* values_f16, uint8_t* is_24);
+
+/* Host-only CSR -> BCSR (no device needed): the block structure that
+ * smat_bcsr_create uploads, bit-identical to SparseMatrix::csrToBcsr
+ * (matrix.h:666-792) on the (optionally permuted) CSR. Call once with
+ * row_ptr == NULL to get *nnzb, then again with row_ptr[rows_padded/bh + 1],
+ * col_idx[nnzb] and values_f16[nnzb*bh*bw]. */
+smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t block_cols,
+                                  const int64_t* row_perm, int64_t* nnzb, int32_t* row_ptr,
+                                  int32_t* col_idx, uint16_t* values_f16);
+
+/* ---------------------------------------------------------------- step 3 */
+
+/* Bytes of device scratch smat_spmm needs for this form / B dtype / N
+ * (0 when B is used in place). */
+smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
+                                     size_t* bytes);
+
+/* C = A * B on the tensor cores. Replaces the launchers with the
+ * HGEMM_FUNC_SPARSE2 / HGEMM_FUNC_SPARSE24_2 signatures
+ * (src/cuda_hgemm/src/main.cu:20-28; mmaOBT.cu:160-169, mmaOBTS_large.cu:256-266).
+ *  B (device): K x N, K = A's column count; element (k, n) at
+ *     B[k + n*ldb] (SMAT_COL_MAJOR, the reference layout) or
+ *     B[k*ldb + n] (SMAT_ROW_MAJOR). b_dtype: F16 for SMAT_FORM_F16, BF16 for
+ *     SMAT_FORM_BF16, or F32 for any form (converted on the fly into workspace).
+ *  C (device): rows x N, row-major, C[i*ldc + n], c_dtype F32 or F16; rows
+ *     in the ORIGINAL order when the handle was built with row_perm.
+ *  workspace (device): smat_spmm_workspace_size() bytes, 256-byte aligned. */
+smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                      int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
+                      int64_t N, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Host-buffer variant: copies B (host) in, runs smat_spmm, copies C (host)
+ * out, and waits for completion. Uses device buffers cached in the handle. */
+smat_status smat_spmm_host(const smat_bcsr* A, int32_t form, const void* B_host, int32_t b_dtype,
+                           int32_t b_layout, int64_t ldb, void* C_host, int32_t c_dtype,
+                           int64_t ldc, int64_t N, void* stream);
+
+/* Reads and clears the handle's device-side error word, which the kernels
+ * set when a bounded wait expires (then SMAT_ERR_TIMEOUT is returned). Call
+ * after synchronising the stream the SpMM ran on. */
+smat_status smat_bcsr_check_device_error(const smat_bcsr* A);
+
+const char* smat_last_error(void);
+const char* smat_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMAT_H_ */

@@ -1,0 +1,528 @@
+// api.cu — the C ABI declared in include/smat.h.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "convert.h"
+#include "fp_convert.h"
+#include "smat_internal.h"
+#include "spmm_tc.h"
+
+namespace smat {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+smat_status fail(smat_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+static smat_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(SMAT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SMAT_CUDA(call)                               \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// RAII: make `dev` current, restore the caller's device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// 2-D tiled map over a 16-bit matrix whose rows of `inner` elements are
+// `row_bytes` apart; box = box_inner x box_outer; 32-byte swizzle.
+static smat_status encode_2d_u16(CUtensorMap* tm, CUtensorMapDataType dt, const void* base,
+                                 uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                                 uint32_t box_inner, uint32_t box_outer) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return fail(SMAT_ERR_NO_DEVICE, "cuTensorMapEncodeTiled not available");
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (row_bytes & 15))
+    return fail(SMAT_ERR_INVALID, "TMA operand must be 16-byte aligned with 16-byte row pitch");
+  if (inner == 0 || outer == 0) return fail(SMAT_ERR_INVALID, "empty TMA operand");
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {row_bytes};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(tm, dt, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(SMAT_ERR_INVALID, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return SMAT_OK;
+}
+
+template <typename T>
+static smat_status upload(T** dptr, const T* src, size_t n) {
+  *dptr = nullptr;
+  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  SMAT_CUDA(cudaMalloc(reinterpret_cast<void**>(dptr), bytes));
+  if (n) SMAT_CUDA(cudaMemcpy(*dptr, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return SMAT_OK;
+}
+
+}  // namespace smat
+
+using namespace smat;
+
+struct Sched {
+  int grid = 0;
+  int32_t* d_cta_ptr = nullptr;
+  int32_t* d_cta_items = nullptr;
+};
+
+struct smat_bcsr {
+  int device = 0;
+  HostBcsr host;
+  Plan plan;
+  uint32_t forms = 0;
+  int use24 = 0;
+  int64_t n_24 = 0;
+  int num_sms = 0;
+  int32_t *d_rowptr = nullptr, *d_row_map = nullptr, *d_ucol_ptr = nullptr, *d_ucol = nullptr,
+          *d_ublk_ptr = nullptr;
+  uint32_t* d_ublk = nullptr;
+  Sched sched[3];  // by NSUB (1, 2)
+  uint16_t* d_val[4] = {nullptr, nullptr, nullptr, nullptr};  // F16, BF16, -, SPLIT hi
+  uint16_t* d_val_lo = nullptr;
+  CUtensorMap tm_val[4];
+  CUtensorMap tm_lo;
+  int* d_err = nullptr;
+  // smat_spmm_host staging
+  std::mutex mu;
+  void* d_bstage = nullptr;
+  size_t bstage_bytes = 0;
+  void* d_cstage = nullptr;
+  size_t cstage_bytes = 0;
+  void* d_ws = nullptr;
+  size_t ws_bytes = 0;
+};
+
+static void free_handle(smat_bcsr* h) {
+  if (!h) return;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(h->device);
+  void* ptrs[] = {h->d_rowptr, h->d_row_map, h->d_ucol_ptr, h->d_ucol, h->d_ublk_ptr, h->d_ublk,
+                  h->d_val[0], h->d_val[1], h->d_val[2], h->d_val[3], h->d_val_lo, h->d_err,
+                  h->d_bstage, h->d_cstage, h->d_ws, h->sched[1].d_cta_ptr, h->sched[1].d_cta_items,
+                  h->sched[2].d_cta_ptr, h->sched[2].d_cta_items};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete h;
+}
+
+static int pick_nsub(const smat_bcsr* h, int64_t N, bool split) {
+  if (N > 128 && tc_variant_supported(h->host.bh, h->plan.R, 2, split)) return 2;
+  return 1;
+}
+
+extern "C" {
+
+const char* smat_last_error(void) { return g_last_error.c_str(); }
+const char* smat_version(void) { return "smat-gb300 0.1 (sm_103a, tcgen05)"; }
+
+smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
+                         int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
+                         int64_t* grouping_out, smat_reorder_stats* stats) {
+  (void)use_gpu;
+  if (!A || !perm_out) return fail(SMAT_ERR_INVALID, "null argument");
+  if (A->rows < 0 || !A->row_ptr || (A->nnz > 0 && !A->col_idx))
+    return fail(SMAT_ERR_INVALID, "malformed CSR");
+  if (col_block < 1 || row_block < 1) return fail(SMAT_ERR_INVALID, "block sizes must be >= 1");
+  if (A->row_ptr[0] != 0 || A->row_ptr[A->rows] != A->nnz)
+    return fail(SMAT_ERR_INVALID, "row_ptr[0] must be 0 and row_ptr[rows] == nnz");
+  for (int64_t r = 0; r < A->rows; r++)
+    if (A->row_ptr[r + 1] < A->row_ptr[r]) return fail(SMAT_ERR_INVALID, "row_ptr not monotone");
+  for (int64_t k = 0; k < A->nnz; k++)
+    if (A->col_idx[k] < 0) return fail(SMAT_ERR_INVALID, "negative column index");
+  std::vector<int64_t> g;
+  int64_t comparisons = 0, merges = 0;
+  if (algo == 5) {
+    keeper_grouping_host(A->rows, A->row_ptr, A->col_idx, tau, col_block, row_block, g,
+                         comparisons, merges);
+  } else if (algo == 2) {
+    // FixedBlocking (blocking.cpp:551-559)
+    g.resize(A->rows);
+    for (int64_t i = 0; i < A->rows; i++) g[i] = i / row_block;
+  } else {
+    return fail(SMAT_ERR_UNSUPPORTED, "only algorithms 5 (Keeper) and 2 (fixed) are implemented");
+  }
+  if (force_fixed && algo != 2) g = fixed_size_grouping(g, row_block);
+  std::vector<int64_t> p = permutation_of(g);
+  std::copy(p.begin(), p.end(), perm_out);
+  if (grouping_out) std::copy(g.begin(), g.end(), grouping_out);
+  if (stats) {
+    stats->comparisons = comparisons;
+    stats->merges = merges;
+  }
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat_bcsr** out) {
+  if (!A || !out) return fail(SMAT_ERR_INVALID, "null argument");
+  *out = nullptr;
+  smat_bcsr_opts o{};
+  if (opts) o = *opts;
+  const int bh = o.block_rows ? o.block_rows : 16;
+  const int bw = o.block_cols ? o.block_cols : 16;
+  if (bw != 16 || (bh != 16 && bh != 32))
+    return fail(SMAT_ERR_UNSUPPORTED, "tensor-core path supports 16x16 and 32x16 blocks");
+  uint32_t forms = o.forms ? o.forms : (1u << SMAT_FORM_F16);
+  if (forms & (1u << SMAT_FORM_FP8)) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(SMAT_ERR_NO_DEVICE, "no CUDA device");
+  if (o.device < 0 || o.device >= ndev) return fail(SMAT_ERR_INVALID, "bad device ordinal");
+  DeviceGuard guard(o.device);
+  if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+  cudaDeviceProp prop;
+  SMAT_CUDA(cudaGetDeviceProperties(&prop, o.device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(SMAT_ERR_NO_DEVICE, "libsmat kernels are built for sm_103a (GB300) only");
+
+  smat_bcsr* h = new smat_bcsr();
+  h->device = o.device;
+  h->forms = forms;
+  h->use24 = o.use_24;
+  h->num_sms = prop.multiProcessorCount;
+  smat_status st = build_host_bcsr(*A, bh, bw, o.row_perm, h->host);
+  if (st != SMAT_OK) {
+    delete h;
+    return st;
+  }
+  int R = o.panel_rows ? o.panel_rows : (bh == 16 ? 8 : 4);
+  if (!tc_variant_supported(bh, R, 1, false)) {
+    delete h;
+    return fail(SMAT_ERR_UNSUPPORTED, "unsupported panel_rows for this block height");
+  }
+  st = build_plan(h->host, R, h->plan);
+  if (st != SMAT_OK) {
+    delete h;
+    return st;
+  }
+  for (uint8_t v : h->host.is24) h->n_24 += v;
+  if (!h->use24) h->n_24 = 0;
+
+#define SMAT_TRY(x)              \
+  do {                           \
+    smat_status s_ = (x);        \
+    if (s_ != SMAT_OK) {         \
+      free_handle(h);            \
+      return s_;                 \
+    }                            \
+  } while (0)
+
+  const HostBcsr& b = h->host;
+  SMAT_TRY(upload(&h->d_rowptr, b.rowptr.data(), b.rowptr.size()));
+  SMAT_TRY(upload(&h->d_row_map, b.row_map.data(), b.row_map.size()));
+  SMAT_TRY(upload(&h->d_ucol_ptr, h->plan.ucol_ptr.data(), h->plan.ucol_ptr.size()));
+  SMAT_TRY(upload(&h->d_ucol, h->plan.ucol.data(), h->plan.ucol.size()));
+  SMAT_TRY(upload(&h->d_ublk_ptr, h->plan.ublk_ptr.data(), h->plan.ublk_ptr.size()));
+  SMAT_TRY(upload(&h->d_ublk, h->plan.ublk.data(), h->plan.ublk.size()));
+  {
+    int zero = 0;
+    SMAT_TRY(upload(&h->d_err, &zero, 1));
+  }
+
+  // per-panel cost: A bytes + B tile bytes (mostly L2 hits) + C bytes written
+  const int64_t nnzb = b.nnzb();
+  std::vector<double> cost(h->plan.n_panels);
+  for (int32_t p = 0; p < h->plan.n_panels; p++) {
+    double blocks = h->plan.ucol_ptr[p + 1] > h->plan.ucol_ptr[p]
+                        ? (double)(h->plan.ublk_ptr[h->plan.ucol_ptr[p + 1]] - h->plan.ublk_ptr[h->plan.ucol_ptr[p]])
+                        : 0.0;
+    double ucols = h->plan.ucol_ptr[p + 1] - h->plan.ucol_ptr[p];
+    cost[p] = blocks * bh * 32.0 + ucols * 128 * 32 * 0.5 + (double)R * bh * 128 * 4 + 2048;
+  }
+  for (int nsub = 1; nsub <= 2; nsub++) {
+    if (!tc_variant_supported(bh, R, nsub, false)) continue;
+    int per_sm = tc_ctas_per_sm(bh, R, nsub, false);
+    int workers = std::max(1, std::min(h->plan.n_panels, h->num_sms * per_sm));
+    std::vector<int32_t> cta_ptr, cta_items;
+    assign_items(cost, workers, cta_ptr, cta_items);
+    h->sched[nsub].grid = workers;
+    SMAT_TRY(upload(&h->sched[nsub].d_cta_ptr, cta_ptr.data(), cta_ptr.size()));
+    SMAT_TRY(upload(&h->sched[nsub].d_cta_items, cta_items.data(), cta_items.size()));
+  }
+
+  // values, one device copy per requested form
+  const size_t nval = (size_t)nnzb * bh * bw;
+  const uint64_t rows_of_blocks = (uint64_t)std::max<int64_t>(nnzb, 1) * bh;
+  if (forms & (1u << SMAT_FORM_F16)) {
+    SMAT_TRY(upload(&h->d_val[SMAT_FORM_F16], b.val_f16.data(), nval));
+    SMAT_TRY(encode_2d_u16(&h->tm_val[SMAT_FORM_F16], CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                           h->d_val[SMAT_FORM_F16], 16, rows_of_blocks, 32, 16, bh));
+  }
+  if (forms & ((1u << SMAT_FORM_BF16) | (1u << SMAT_FORM_SPLIT_BF16))) {
+    std::vector<uint16_t> hi(nval), lo(nval);
+    for (size_t i = 0; i < nval; i++) {
+      hi[i] = f32_to_bf16_bits(b.val[i]);
+      lo[i] = f32_to_bf16_bits(b.val[i] - bf16_bits_to_f32(hi[i]));
+    }
+    if (forms & (1u << SMAT_FORM_BF16)) {
+      SMAT_TRY(upload(&h->d_val[SMAT_FORM_BF16], hi.data(), nval));
+      SMAT_TRY(encode_2d_u16(&h->tm_val[SMAT_FORM_BF16], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                             h->d_val[SMAT_FORM_BF16], 16, rows_of_blocks, 32, 16, bh));
+    }
+    if (forms & (1u << SMAT_FORM_SPLIT_BF16)) {
+      SMAT_TRY(upload(&h->d_val[SMAT_FORM_SPLIT_BF16], hi.data(), nval));
+      SMAT_TRY(upload(&h->d_val_lo, lo.data(), nval));
+      SMAT_TRY(encode_2d_u16(&h->tm_val[SMAT_FORM_SPLIT_BF16], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                             h->d_val[SMAT_FORM_SPLIT_BF16], 16, rows_of_blocks, 32, 16, bh));
+      SMAT_TRY(encode_2d_u16(&h->tm_lo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, h->d_val_lo, 16,
+                             rows_of_blocks, 32, 16, bh));
+    }
+  }
+  // keep the FP16 values for export; the FP32 copy is no longer needed
+  std::vector<float>().swap(h->host.val);
+#undef SMAT_TRY
+  *out = h;
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_destroy(smat_bcsr* A) {
+  free_handle(A);
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info) {
+  if (!A || !info) return fail(SMAT_ERR_INVALID, "null argument");
+  const HostBcsr& b = A->host;
+  info->rows = b.rows;
+  info->cols = b.cols;
+  info->rows_padded = b.rows_p;
+  info->cols_padded = b.cols_p;
+  info->nnz = b.nnz;
+  info->nnzb = b.nnzb();
+  info->n_blocks_24 = A->n_24;
+  info->block_rows = b.bh;
+  info->block_cols = b.bw;
+  info->panel_rows = A->plan.R;
+  info->n_panels = A->plan.n_panels;
+  info->n_union_cols = (int64_t)A->plan.ucol.size();
+  info->fill = b.nnzb() ? (double)b.nnz / ((double)b.nnzb() * b.bh * b.bw) : 0.0;
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_export(const smat_bcsr* A, int32_t* row_ptr, int32_t* col_idx,
+                             uint16_t* values_f16, uint8_t* is_24) {
+  if (!A) return fail(SMAT_ERR_INVALID, "null argument");
+  const HostBcsr& b = A->host;
+  if (row_ptr) std::copy(b.rowptr.begin(), b.rowptr.end(), row_ptr);
+  if (col_idx) std::copy(b.colidx.begin(), b.colidx.end(), col_idx);
+  if (values_f16) std::copy(b.val_f16.begin(), b.val_f16.end(), values_f16);
+  if (is_24) std::copy(b.is24.begin(), b.is24.end(), is_24);
+  return SMAT_OK;
+}
+
+smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t block_cols,
+                                  const int64_t* row_perm, int64_t* nnzb, int32_t* row_ptr,
+                                  int32_t* col_idx, uint16_t* values_f16) {
+  if (!A || !nnzb) return fail(SMAT_ERR_INVALID, "null argument");
+  HostBcsr b;
+  smat_status st = build_host_bcsr(*A, block_rows ? block_rows : 16, block_cols ? block_cols : 16,
+                                   row_perm, b);
+  if (st != SMAT_OK) return st;
+  *nnzb = b.nnzb();
+  if (row_ptr) std::copy(b.rowptr.begin(), b.rowptr.end(), row_ptr);
+  if (col_idx) std::copy(b.colidx.begin(), b.colidx.end(), col_idx);
+  if (values_f16) std::copy(b.val_f16.begin(), b.val_f16.end(), values_f16);
+  return SMAT_OK;
+}
+
+static bool b_in_place(int32_t form, int32_t b_dtype, int32_t b_layout, const void* B, int64_t ldb) {
+  const bool dt_ok = (form == SMAT_FORM_F16 && b_dtype == SMAT_F16) ||
+                     (form == SMAT_FORM_BF16 && b_dtype == SMAT_BF16);
+  return dt_ok && b_layout == SMAT_COL_MAJOR && (ldb % 8) == 0 &&
+         (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+}
+
+smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
+                                     size_t* bytes) {
+  if (!A || !bytes) return fail(SMAT_ERR_INVALID, "null argument");
+  const int64_t ldo = (A->host.cols_p + 7) / 8 * 8;
+  const size_t one = ((size_t)ldo * (size_t)std::max<int64_t>(N, 1) * 2 + 255) / 256 * 256;
+  (void)b_dtype;
+  *bytes = (form == SMAT_FORM_SPLIT_BF16) ? 2 * one : one;
+  return SMAT_OK;
+}
+
+smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                      int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
+                      int64_t N, void* workspace, size_t workspace_bytes, void* stream_) {
+  if (!A || !B || !C) return fail(SMAT_ERR_INVALID, "null argument");
+  if (form < 0 || form > 3 || !(A->forms & (1u << form)))
+    return fail(SMAT_ERR_INVALID, "form was not materialised when the handle was built");
+  if (form == SMAT_FORM_FP8) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
+  if (N <= 0 || N > (1 << 30)) return fail(SMAT_ERR_INVALID, "bad N");
+  if (c_dtype != SMAT_F32 && c_dtype != SMAT_F16) return fail(SMAT_ERR_INVALID, "C must be F32 or F16");
+  if (ldc < N) return fail(SMAT_ERR_INVALID, "ldc < N");
+  if (b_layout != SMAT_ROW_MAJOR && b_layout != SMAT_COL_MAJOR) return fail(SMAT_ERR_INVALID, "bad B layout");
+  if (b_dtype != SMAT_F32 && b_dtype != SMAT_F16 && b_dtype != SMAT_BF16)
+    return fail(SMAT_ERR_INVALID, "B must be F32, F16 or BF16");
+  const HostBcsr& hb = A->host;
+  const int64_t K = hb.cols;
+  if (b_layout == SMAT_COL_MAJOR ? ldb < K : ldb < N) return fail(SMAT_ERR_INVALID, "ldb too small");
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  DeviceGuard guard(A->device);
+  if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+
+  const bool split = form == SMAT_FORM_SPLIT_BF16;
+  const int nsub = pick_nsub(A, N, split);
+  const int bh = hb.bh, R = A->plan.R;
+  if (!tc_variant_supported(bh, R, nsub, split)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
+  const Sched& sc = A->sched[nsub];
+
+  SpmmArgs args;
+  std::memset(&args, 0, sizeof(args));
+  const CUtensorMapDataType bdt =
+      (form == SMAT_FORM_F16) ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  const uint32_t BN = 128u * nsub;
+  const void* Bdev = B;
+  int64_t ldo = ldb;
+  if (!b_in_place(form, b_dtype, b_layout, B, ldb)) {
+    size_t need = 0;
+    smat_spmm_workspace_size(A, form, b_dtype, N, &need);
+    if (!workspace || workspace_bytes < need)
+      return fail(SMAT_ERR_INVALID, "workspace too small (see smat_spmm_workspace_size)");
+    if (reinterpret_cast<uintptr_t>(workspace) & 255) return fail(SMAT_ERR_INVALID, "workspace must be 256-byte aligned");
+    ldo = (hb.cols_p + 7) / 8 * 8;
+    uint16_t* hi = static_cast<uint16_t*>(workspace);
+    uint16_t* lo = split ? hi + need / 4 : nullptr;
+    const int in_dt = b_dtype == SMAT_F32 ? 0 : (b_dtype == SMAT_F16 ? 1 : 2);
+    const int mode = form == SMAT_FORM_F16 ? 0 : (split ? 2 : 1);
+    cudaError_t e = convert_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, hi, lo, ldo,
+                              K, N, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "convert_b");
+    Bdev = hi;
+    if (split) {
+      smat_status s = encode_2d_u16(&args.tmB2, bdt, lo, (uint64_t)K, (uint64_t)N, (uint64_t)ldo * 2, 16, BN);
+      if (s != SMAT_OK) return s;
+    }
+  }
+  smat_status s = encode_2d_u16(&args.tmB, bdt, Bdev, (uint64_t)K, (uint64_t)N, (uint64_t)ldo * 2, 16, BN);
+  if (s != SMAT_OK) return s;
+  args.tmA = A->tm_val[form];
+  if (split) args.tmA2 = A->tm_lo;
+  args.rowptr = A->d_rowptr;
+  args.ucol_ptr = A->d_ucol_ptr;
+  args.ucol = A->d_ucol;
+  args.ublk_ptr = A->d_ublk_ptr;
+  args.ublk = A->d_ublk;
+  args.cta_ptr = sc.d_cta_ptr;
+  args.cta_items = sc.d_cta_items;
+  args.row_map = A->d_row_map;
+  args.C = C;
+  args.ldc = ldc;
+  args.N = (int32_t)N;
+  args.n_tiles = (int32_t)((N + BN - 1) / BN);
+  args.nbr = (int32_t)hb.nbr();
+  args.c_f16 = c_dtype == SMAT_F16;
+  args.idesc = (form == SMAT_FORM_F16) ? 0x0u : 0x0u;
+  {
+    const uint32_t fmt = (form == SMAT_FORM_F16) ? 0u : 1u;
+    args.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(bh >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  }
+  args.err = A->d_err;
+  if (A->plan.n_panels == 0 || hb.rows == 0) {
+    // empty matrix: C = 0
+    for (int64_t i = 0; i < hb.rows; i++) {
+      cudaError_t e = cudaMemsetAsync(static_cast<char*>(C) + i * ldc * (c_dtype == SMAT_F16 ? 2 : 4), 0,
+                                      N * (c_dtype == SMAT_F16 ? 2 : 4), stream);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    return SMAT_OK;
+  }
+  cudaError_t e = tc_launch(bh, R, nsub, split, args, sc.grid, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "spmm kernel launch");
+  return SMAT_OK;
+}
+
+smat_status smat_spmm_host(const smat_bcsr* A_, int32_t form, const void* B_host, int32_t b_dtype,
+                           int32_t b_layout, int64_t ldb, void* C_host, int32_t c_dtype,
+                           int64_t ldc, int64_t N, void* stream_) {
+  if (!A_ || !B_host || !C_host) return fail(SMAT_ERR_INVALID, "null argument");
+  smat_bcsr* A = const_cast<smat_bcsr*>(A_);
+  std::lock_guard<std::mutex> lock(A->mu);
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  DeviceGuard guard(A->device);
+  const int64_t K = A->host.cols, M = A->host.rows;
+  const size_t belt = b_dtype == SMAT_F32 ? 4 : 2, celt = c_dtype == SMAT_F16 ? 2 : 4;
+  const size_t bbytes = (b_layout == SMAT_COL_MAJOR) ? (size_t)ldb * (N - 1) * belt + K * belt
+                                                     : (size_t)ldb * (K - 1) * belt + N * belt;
+  const size_t cbytes = (size_t)ldc * (M - 1) * celt + N * celt;
+  size_t wbytes = 0;
+  smat_spmm_workspace_size(A, form, b_dtype, N, &wbytes);
+  auto grow = [](void** p, size_t* cap, size_t need) -> cudaError_t {
+    if (*cap >= need) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, need);
+    if (e == cudaSuccess) *cap = need;
+    return e;
+  };
+  SMAT_CUDA(grow(&A->d_bstage, &A->bstage_bytes, bbytes));
+  SMAT_CUDA(grow(&A->d_cstage, &A->cstage_bytes, std::max<size_t>(cbytes, 1)));
+  SMAT_CUDA(grow(&A->d_ws, &A->ws_bytes, wbytes));
+  SMAT_CUDA(cudaMemcpyAsync(A->d_bstage, B_host, bbytes, cudaMemcpyHostToDevice, stream));
+  smat_status s = smat_spmm(A, form, A->d_bstage, b_dtype, b_layout, ldb, A->d_cstage, c_dtype, ldc,
+                            N, A->d_ws, A->ws_bytes, stream);
+  if (s != SMAT_OK) return s;
+  SMAT_CUDA(cudaMemcpyAsync(C_host, A->d_cstage, cbytes, cudaMemcpyDeviceToHost, stream));
+  SMAT_CUDA(cudaStreamSynchronize(stream));
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_check_device_error(const smat_bcsr* A) {
+  if (!A) return fail(SMAT_ERR_INVALID, "null argument");
+  DeviceGuard guard(A->device);
+  int v = 0;
+  SMAT_CUDA(cudaMemcpy(&v, A->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v != 0) {
+    int zero = 0;
+    cudaMemcpy(A->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return fail(SMAT_ERR_TIMEOUT, "device-side wait timed out at site " + std::to_string(v));
+  }
+  return SMAT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,255 @@
+// bcsr.cpp — CSR -> BCSR on the host, and the tensor-core work plan.
+//
+// The block structure is bit-identical to SparseMatrix::csrToBcsr
+// (src/cuda_hgemm/src/common/matrix.h:666-792): per block row the nonzero
+// block columns in ascending order, bcsrColIdx = the column START of the
+// block, values row-major inside a block, zero-filled, the last CSR entry of
+// a duplicated (row, col) winning. Unlike the reference it does not allocate
+// the dense (rows/bh) x (cols/bw) block grid (1 GiB per array for a 256K x
+// 256K matrix); it works block row by block row with a stamp array.
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "fp_convert.h"
+#include "smat_internal.h"
+
+namespace smat {
+
+smat_status build_host_bcsr(const smat_csr& A, int32_t bh, int32_t bw, const int64_t* perm,
+                            HostBcsr& out) {
+  if (A.rows < 0 || A.cols < 0 || A.nnz < 0) return fail(SMAT_ERR_INVALID, "negative CSR size");
+  if (!A.row_ptr || (A.nnz > 0 && !A.col_idx)) return fail(SMAT_ERR_INVALID, "CSR arrays missing");
+  if (A.values && A.values_dtype != SMAT_F32 && A.values_dtype != SMAT_F16 &&
+      A.values_dtype != SMAT_F64)
+    return fail(SMAT_ERR_INVALID, "CSR values must be F32, F16 or F64");
+  if (!(bh == 8 || bh == 16 || bh == 32) || !(bw == 8 || bw == 16 || bw == 32))
+    return fail(SMAT_ERR_UNSUPPORTED, "block shape must be 8, 16 or 32 on each side");
+  if (A.row_ptr[0] != 0 || A.row_ptr[A.rows] != A.nnz)
+    return fail(SMAT_ERR_INVALID, "row_ptr[0] must be 0 and row_ptr[rows] == nnz");
+  for (int64_t r = 0; r < A.rows; r++)
+    if (A.row_ptr[r + 1] < A.row_ptr[r]) return fail(SMAT_ERR_INVALID, "row_ptr not monotone");
+  for (int64_t k = 0; k < A.nnz; k++)
+    if (A.col_idx[k] < 0 || A.col_idx[k] >= A.cols)
+      return fail(SMAT_ERR_INVALID, "column index out of range");
+  if (perm) {
+    std::vector<uint8_t> seen(A.rows, 0);
+    for (int64_t r = 0; r < A.rows; r++) {
+      if (perm[r] < 0 || perm[r] >= A.rows || seen[perm[r]])
+        return fail(SMAT_ERR_INVALID, "row_perm is not a permutation");
+      seen[perm[r]] = 1;
+    }
+  }
+  out.rows = A.rows;
+  out.cols = A.cols;
+  out.bh = bh;
+  out.bw = bw;
+  out.nnz = A.nnz;
+  out.rows_p = (A.rows + bh - 1) / bh * bh;
+  out.cols_p = (A.cols + bw - 1) / bw * bw;
+  const int64_t nbr = out.rows_p / bh, nbc = out.cols_p / bw;
+  if (out.cols_p > INT32_MAX) return fail(SMAT_ERR_UNSUPPORTED, "more than 2^31 columns");
+
+  out.row_map.assign(out.rows_p, -1);
+  for (int64_t r = 0; r < A.rows; r++) out.row_map[r] = (int32_t)(perm ? perm[r] : r);
+
+  auto src_row = [&](int64_t r) -> int64_t { return perm ? perm[r] : r; };
+
+  // pass 1: number of nonzero blocks per block row
+  std::vector<int64_t> cnt(nbr + 1, 0);
+#pragma omp parallel
+  {
+    std::vector<int64_t> stamp(nbc, -1);
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t br = 0; br < nbr; br++) {
+      int64_t c = 0;
+      for (int64_t r = br * bh; r < std::min<int64_t>((br + 1) * bh, A.rows); r++) {
+        int64_t s = src_row(r);
+        for (int64_t k = A.row_ptr[s]; k < A.row_ptr[s + 1]; k++) {
+          int64_t bc = A.col_idx[k] / bw;
+          if (stamp[bc] != br) {
+            stamp[bc] = br;
+            c++;
+          }
+        }
+      }
+      cnt[br + 1] = c;
+    }
+  }
+  for (int64_t br = 0; br < nbr; br++) cnt[br + 1] += cnt[br];
+  const int64_t nnzb = cnt[nbr];
+  if (nnzb > INT32_MAX / 2) return fail(SMAT_ERR_UNSUPPORTED, "too many blocks");
+  out.rowptr.resize(nbr + 1);
+  for (int64_t br = 0; br <= nbr; br++) out.rowptr[br] = (int32_t)cnt[br];
+  out.colidx.resize(nnzb);
+  const int64_t bsz = (int64_t)bh * bw;
+  out.val.assign(nnzb * bsz, 0.0f);
+  out.val_f16.assign(nnzb * bsz, 0);
+  out.is24.assign(nnzb, 0);
+
+  // pass 2: sorted block columns, then values in CSR order
+#pragma omp parallel
+  {
+    std::vector<int64_t> stamp(nbc, -1);
+    std::vector<int32_t> slot(nbc, 0);
+    std::vector<int32_t> cols;
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t br = 0; br < nbr; br++) {
+      cols.clear();
+      const int64_t r1 = std::min<int64_t>((br + 1) * bh, A.rows);
+      for (int64_t r = br * bh; r < r1; r++) {
+        int64_t s = src_row(r);
+        for (int64_t k = A.row_ptr[s]; k < A.row_ptr[s + 1]; k++) {
+          int64_t bc = A.col_idx[k] / bw;
+          if (stamp[bc] != br) {
+            stamp[bc] = br;
+            cols.push_back((int32_t)bc);
+          }
+        }
+      }
+      std::sort(cols.begin(), cols.end());
+      const int64_t base = cnt[br];
+      for (size_t t = 0; t < cols.size(); t++) {
+        out.colidx[base + t] = cols[t] * bw;
+        slot[cols[t]] = (int32_t)(base + t);
+      }
+      for (int64_t r = br * bh; r < r1; r++) {
+        int64_t s = src_row(r);
+        for (int64_t k = A.row_ptr[s]; k < A.row_ptr[s + 1]; k++) {
+          int64_t col = A.col_idx[k];
+          int64_t b = slot[col / bw];
+          int64_t off = b * bsz + (r % bh) * bw + col % bw;
+          float vf;
+          uint16_t vh;
+          if (!A.values) {
+            vf = 1.0f;
+            vh = 0x3c00;
+          } else if (A.values_dtype == SMAT_F32) {
+            vf = ((const float*)A.values)[k];
+            vh = f32_to_f16_bits(vf);
+          } else if (A.values_dtype == SMAT_F64) {
+            double d = ((const double*)A.values)[k];
+            vf = (float)d;
+            vh = f64_to_f16_bits(d);
+          } else {
+            vh = ((const uint16_t*)A.values)[k];
+            vf = f16_bits_to_f32(vh);
+          }
+          out.val[off] = vf;
+          out.val_f16[off] = vh;
+        }
+      }
+      // exact 2:4 along the block's columns, judged on the FP16 values
+      for (int64_t b = base; b < cnt[br + 1]; b++) {
+        const uint16_t* v = out.val_f16.data() + b * bsz;
+        bool ok = (bw % 4) == 0;
+        for (int rr = 0; rr < bh && ok; rr++)
+          for (int g = 0; g < bw && ok; g += 4) {
+            int nz = 0;
+            for (int c = g; c < g + 4; c++) nz += (v[rr * bw + c] & 0x7fff) != 0;
+            ok = nz <= 2;
+          }
+        out.is24[b] = ok ? 1 : 0;
+      }
+    }
+  }
+  return SMAT_OK;
+}
+
+smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
+  if (R < 1 || R > 32) return fail(SMAT_ERR_INVALID, "panel rows must be in [1, 32]");
+  const int64_t nbr = b.nbr();
+  plan.R = R;
+  plan.n_panels = (int32_t)((nbr + R - 1) / R);
+  const int32_t P = plan.n_panels;
+  std::vector<int64_t> ucnt(P + 1, 0), bcnt(P + 1, 0);
+  // pass 1: union sizes
+#pragma omp parallel
+  {
+    std::vector<int32_t> cols;
+#pragma omp for schedule(dynamic, 16)
+    for (int32_t p = 0; p < P; p++) {
+      cols.clear();
+      const int64_t br0 = (int64_t)p * R, br1 = std::min<int64_t>(nbr, br0 + R);
+      for (int64_t br = br0; br < br1; br++)
+        for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) cols.push_back(b.colidx[k]);
+      std::sort(cols.begin(), cols.end());
+      ucnt[p + 1] = std::unique(cols.begin(), cols.end()) - cols.begin();
+      bcnt[p + 1] = b.rowptr[br1] - b.rowptr[br0];
+    }
+  }
+  for (int32_t p = 0; p < P; p++) {
+    ucnt[p + 1] += ucnt[p];
+    bcnt[p + 1] += bcnt[p];
+  }
+  if (b.nnzb() >= (int64_t)1 << 27) return fail(SMAT_ERR_UNSUPPORTED, "more than 2^27 blocks");
+  plan.ucol_ptr.resize(P + 1);
+  for (int32_t p = 0; p <= P; p++) plan.ucol_ptr[p] = (int32_t)ucnt[p];
+  plan.ucol.resize(ucnt[P]);
+  plan.ublk_ptr.resize(ucnt[P] + 1);
+  plan.ublk.resize(bcnt[P]);
+  plan.panel_cost.resize(P);
+  // pass 2: per panel, blocks ordered by (column, slot)
+#pragma omp parallel
+  {
+    std::vector<std::pair<int64_t, uint32_t>> ent;  // key = col * 32 + slot
+#pragma omp for schedule(dynamic, 16)
+    for (int32_t p = 0; p < P; p++) {
+      ent.clear();
+      const int64_t br0 = (int64_t)p * R, br1 = std::min<int64_t>(nbr, br0 + R);
+      for (int64_t br = br0; br < br1; br++)
+        for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++)
+          ent.push_back({(int64_t)b.colidx[k] * 32 + (br - br0), ((uint32_t)k << 5) | (uint32_t)(br - br0)});
+      std::sort(ent.begin(), ent.end());
+      int64_t u = ucnt[p], e = bcnt[p];
+      int64_t last_col = -1;
+      for (auto& x : ent) {
+        int64_t col = x.first / 32;
+        if (col != last_col) {
+          plan.ucol[u] = (int32_t)col;
+          plan.ublk_ptr[u] = (int32_t)e;
+          u++;
+          last_col = col;
+        }
+        plan.ublk[e++] = x.second;
+      }
+      plan.panel_cost[p] = 0;  // filled by the launcher for its tile width
+    }
+  }
+  plan.ublk_ptr[ucnt[P]] = (int32_t)bcnt[P];
+  return SMAT_OK;
+}
+
+void assign_items(const std::vector<double>& cost, int32_t workers, std::vector<int32_t>& cta_ptr,
+                  std::vector<int32_t>& cta_items) {
+  const int32_t n = (int32_t)cost.size();
+  std::vector<int32_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
+  // min-heap of (load, worker)
+  std::vector<std::pair<double, int32_t>> heap;
+  for (int32_t w = 0; w < workers; w++) heap.push_back({0.0, w});
+  auto cmp = [](const std::pair<double, int32_t>& a, const std::pair<double, int32_t>& b) {
+    return a.first > b.first || (a.first == b.first && a.second > b.second);
+  };
+  std::make_heap(heap.begin(), heap.end(), cmp);
+  std::vector<std::vector<int32_t>> q(workers);
+  for (int32_t it : order) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    auto& w = heap.back();
+    q[w.second].push_back(it);
+    w.first += cost[it];
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  cta_ptr.assign(workers + 1, 0);
+  cta_items.clear();
+  for (int32_t w = 0; w < workers; w++) {
+    cta_items.insert(cta_items.end(), q[w].begin(), q[w].end());
+    cta_ptr[w + 1] = (int32_t)cta_items.size();
+  }
+}
+
+}  // namespace smat

@@ -1,0 +1,71 @@
+// smat_internal.h — shared declarations of libsmat's host side.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "smat.h"
+
+namespace smat {
+
+// Thread-local last-error text behind smat_last_error().
+void set_error(const std::string& msg);
+smat_status fail(smat_status st, const std::string& msg);
+
+// ------------------------------------------------------------------ reorder
+struct ReorderResult {
+  std::vector<int64_t> grouping;
+  std::vector<int64_t> perm;
+  int64_t comparisons = 0;
+  int64_t merges = 0;
+};
+
+// Keeper grouping (blocking.cpp:431-547) on the host, bit-exact.
+void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* cols, float tau,
+                          int64_t col_block, int64_t max_row_block, std::vector<int64_t>& grouping,
+                          int64_t& comparisons, int64_t& merges);
+// get_permutation / get_fixed_size_grouping (utilities.cpp:8-20, 45-54).
+std::vector<int64_t> permutation_of(const std::vector<int64_t>& grouping);
+std::vector<int64_t> fixed_size_grouping(const std::vector<int64_t>& grouping, int64_t row_block);
+
+// ------------------------------------------------------------------ BCSR
+// Host-side BCSR structure (bh x bw blocks), bit-identical to csrToBcsr.
+struct HostBcsr {
+  int64_t rows = 0, cols = 0;        // logical
+  int64_t rows_p = 0, cols_p = 0;    // padded
+  int32_t bh = 16, bw = 16;
+  int64_t nnz = 0;
+  std::vector<int32_t> rowptr;       // nbr + 1
+  std::vector<int32_t> colidx;       // nnzb, column start
+  std::vector<float> val;            // nnzb * bh * bw (exact source values, FP32)
+  std::vector<uint16_t> val_f16;     // same, as the FP16 the reference stores
+  std::vector<int32_t> row_map;      // rows_p: BCSR row -> original row (or -1)
+  std::vector<uint8_t> is24;         // per block: exactly 2:4 (values as FP16)
+  int64_t nnzb() const { return (int64_t)colidx.size(); }
+  int64_t nbr() const { return rows_p / bh; }
+};
+
+smat_status build_host_bcsr(const smat_csr& A, int32_t bh, int32_t bw, const int64_t* row_perm,
+                            HostBcsr& out);
+
+// Work plan of the tensor-core SpMM: panels of `R` block rows; per panel the
+// sorted union of block columns ("union columns"), each with the blocks that
+// use it; per CTA a list of work items (panel, n-tile) balanced by cost.
+struct Plan {
+  int32_t R = 8;
+  int32_t n_panels = 0;
+  std::vector<int32_t> ucol_ptr;     // n_panels + 1
+  std::vector<int32_t> ucol;         // column start of each union column
+  std::vector<int32_t> ublk_ptr;     // n_ucols + 1
+  std::vector<uint32_t> ublk;        // (block index << 5) | slot
+  std::vector<double> panel_cost;    // relative cost of one (panel, n-tile) item
+};
+
+smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);
+
+// Longest-processing-time assignment of items to `workers` queues.
+void assign_items(const std::vector<double>& item_cost, int32_t workers,
+                  std::vector<int32_t>& cta_ptr, std::vector<int32_t>& cta_items);
+
+}  // namespace smat

@@ -1,0 +1,244 @@
+"""smat — Python front end of libsmat, the GB300 SMaT pipeline.
+
+Mirrors the reference's three-step surface:
+
+* ``reorder``   — ``Matrix_Blocking -a 5 ... -F 1 -t tau`` / ``BlockingEngine::GetGrouping``
+  (preprocess/src/general/blocking.cpp:616-657) as driven by ``reorder_using_paolo``
+  (src/reorder.py:107-139), returning the reference's permutation;
+* ``Bcsr``      — the ``SparseMatrix`` constructor (src/cuda_hgemm/src/common/matrix.h:161-246):
+  CSR -> BCSR on the device;
+* ``Bcsr.spmm`` — the SpMM launchers (src/cuda_hgemm/src/main.cu:20-28), on tcgen05 tensor cores.
+
+Every call goes through the C ABI of ``include/smat.h``; there is no Python
+or CPU fallback for the SpMM: without the built library or an sm_103 device
+the calls raise ``SmatError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import (BF16, COL_MAJOR, E4M3, F16, F32, F64, FORM_BF16, FORM_F16, FORM_FP8, FORM_SPLIT_BF16,
+                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrStruct, ReorderStats, SmatError, check, lib, ptr)
+
+__all__ = ["Csr", "Bcsr", "reorder", "csr_to_bcsr_host", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
+           "FORM_FP8", "FORM_SPLIT_BF16", "F32", "F16", "BF16", "F64", "E4M3", "ROW_MAJOR", "COL_MAJOR"]
+
+_VAL_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float16): F16, np.dtype(np.float64): F64}
+
+
+@dataclass
+class Csr:
+    """CSR on the host. Column order inside a row is kept as given."""
+    rows: int
+    cols: int
+    row_ptr: np.ndarray
+    col_idx: np.ndarray
+    values: np.ndarray | None = None
+
+    def __post_init__(self):
+        self.row_ptr = np.ascontiguousarray(self.row_ptr, dtype=np.int64)
+        self.col_idx = np.ascontiguousarray(self.col_idx, dtype=np.int32)
+        if self.values is not None:
+            v = np.asarray(self.values)
+            if v.dtype not in _VAL_DTYPES:
+                v = v.astype(np.float32)
+            self.values = np.ascontiguousarray(v)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.row_ptr[-1]) if len(self.row_ptr) else 0
+
+    def struct(self) -> CsrStruct:
+        s = CsrStruct()
+        s.rows, s.cols, s.nnz = self.rows, self.cols, self.nnz
+        s.row_ptr = self.row_ptr.ctypes.data
+        s.col_idx = self.col_idx.ctypes.data if self.nnz else None
+        if self.values is not None:
+            s.values = self.values.ctypes.data
+            s.values_dtype = _VAL_DTYPES[self.values.dtype]
+        else:
+            s.values = None
+            s.values_dtype = F32
+        return s
+
+    @classmethod
+    def from_scipy(cls, m, keep_order: bool = True) -> "Csr":
+        m = m.tocsr()
+        if not keep_order:
+            m.sort_indices()
+        return cls(m.shape[0], m.shape[1], m.indptr, m.indices, m.data)
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        vals = self.values if self.values is not None else np.ones(self.nnz, np.float32)
+        return sp.csr_matrix((vals, self.col_idx, self.row_ptr), shape=(self.rows, self.cols))
+
+    def permuted(self, perm: np.ndarray) -> "Csr":
+        """Rows reordered: new row r = old row perm[r] (CSR::permute_rows, csr.cpp:65-74)."""
+        perm = np.asarray(perm, np.int64)
+        lens = np.diff(self.row_ptr)[perm]
+        rp = np.zeros(self.rows + 1, np.int64)
+        np.cumsum(lens, out=rp[1:])
+        idx = np.concatenate([np.arange(self.row_ptr[p], self.row_ptr[p + 1]) for p in perm]) if self.rows else \
+            np.zeros(0, np.int64)
+        vals = None if self.values is None else self.values[idx]
+        return Csr(self.rows, self.cols, rp, self.col_idx[idx], vals)
+
+
+@dataclass
+class ReorderResult:
+    perm: np.ndarray
+    grouping: np.ndarray
+    comparisons: int
+    merges: int
+
+
+def reorder(csr: Csr, tau: float = 0.5, col_block: int = 16, row_block: int = 16, algo: int = 5,
+            force_fixed: bool = True, use_gpu: bool = False) -> ReorderResult:
+    """Row reordering with the reference's result: new row r = old row perm[r]."""
+    perm = np.zeros(csr.rows, np.int64)
+    grouping = np.zeros(csr.rows, np.int64)
+    st = ReorderStats()
+    s = csr.struct()
+    check(lib().smat_reorder(C.byref(s), C.c_float(tau), col_block, row_block, algo, 1 if force_fixed else 0,
+                             1 if use_gpu else 0, perm.ctypes.data, grouping.ctypes.data, C.byref(st)))
+    return ReorderResult(perm, grouping, st.comparisons, st.merges)
+
+
+def csr_to_bcsr_host(csr: Csr, block=(16, 16), row_perm=None):
+    """Host-only blocking: (row_ptr, col_idx (column starts), values fp16 [nnzb, bh, bw])."""
+    bh, bw = block
+    perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
+    s = csr.struct()
+    nnzb = C.c_int64()
+    pp = None if perm is None else perm.ctypes.data
+    check(lib().smat_csr_to_bcsr_host(C.byref(s), bh, bw, pp, C.byref(nnzb), None, None, None))
+    n = nnzb.value
+    rows_p = (csr.rows + bh - 1) // bh * bh
+    rp = np.zeros(rows_p // bh + 1, np.int32)
+    ci = np.zeros(max(n, 1), np.int32)
+    vals = np.zeros(max(n, 1) * bh * bw, np.uint16)
+    check(lib().smat_csr_to_bcsr_host(C.byref(s), bh, bw, pp, C.byref(nnzb), rp.ctypes.data, ci.ctypes.data,
+                                      vals.ctypes.data))
+    return rp, ci[:n], vals[: n * bh * bw].view(np.float16).reshape(n, bh, bw)
+
+
+def _torch_layout(t):
+    """(layout, ld) of a 2-D torch tensor viewed as (K, N)."""
+    if t.dim() != 2:
+        raise ValueError("B must be 2-D (K, N)")
+    s0, s1 = t.stride()
+    if s0 == 1 and (s1 >= t.shape[0] or t.shape[1] == 1):
+        return COL_MAJOR, max(s1, t.shape[0])
+    if s1 == 1:
+        return ROW_MAJOR, max(s0, t.shape[1])
+    raise ValueError("B must have a unit stride in one dimension")
+
+
+class Bcsr:
+    """A BCSR matrix resident on one GPU (the reference's ``SparseMatrix``)."""
+
+    def __init__(self, csr: Csr, block=(16, 16), forms=(FORM_F16,), row_perm=None, panel_rows: int = 0,
+                 device: int = 0, use_24: bool = False):
+        o = BcsrOpts()
+        o.block_rows, o.block_cols = block
+        o.forms = 0
+        for f in forms:
+            o.forms |= 1 << f
+        o.use_24 = 1 if use_24 else 0
+        self._perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
+        o.row_perm = None if self._perm is None else self._perm.ctypes.data
+        o.device = device
+        o.panel_rows = panel_rows
+        h = C.c_void_p()
+        s = csr.struct()
+        check(lib().smat_bcsr_create(C.byref(s), C.byref(o), C.byref(h)))
+        self._h = h
+        self.device = device
+        self.forms = tuple(forms)
+        inf = BcsrInfo()
+        check(lib().smat_bcsr_get_info(self._h, C.byref(inf)))
+        self.info = {k: getattr(inf, k) for k, _ in BcsrInfo._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().smat_bcsr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def export(self):
+        """(row_ptr int32, col_idx int32 (column starts), values fp16 [nnzb, bh, bw], is_24 uint8)."""
+        i = self.info
+        nbr = i["rows_padded"] // i["block_rows"]
+        rp = np.zeros(nbr + 1, np.int32)
+        ci = np.zeros(max(i["nnzb"], 1), np.int32)
+        vals = np.zeros(max(i["nnzb"], 1) * i["block_rows"] * i["block_cols"], np.uint16)
+        is24 = np.zeros(max(i["nnzb"], 1), np.uint8)
+        check(lib().smat_bcsr_export(self._h, rp.ctypes.data, ci.ctypes.data, vals.ctypes.data, is24.ctypes.data))
+        n = i["nnzb"]
+        return (rp, ci[:n], vals[: n * i["block_rows"] * i["block_cols"]].view(np.float16)
+                .reshape(n, i["block_rows"], i["block_cols"]), is24[:n])
+
+    def workspace_size(self, form: int, b_dtype: int, N: int) -> int:
+        n = C.c_size_t()
+        check(lib().smat_spmm_workspace_size(self._h, form, b_dtype, N, C.byref(n)))
+        return n.value
+
+    def spmm_raw(self, form, B, b_dtype, b_layout, ldb, Cmat, c_dtype, ldc, N, workspace=None,
+                 workspace_bytes=0, stream=0):
+        """Direct C-ABI call on device pointers (ints or tensors)."""
+        check(lib().smat_spmm(self._h, form, ptr(B), b_dtype, b_layout, ldb, ptr(Cmat), c_dtype, ldc, N,
+                              ptr(workspace), workspace_bytes, stream))
+
+    def spmm(self, B, form: int = FORM_F16, out=None, out_dtype=None, workspace=None, stream=None):
+        """C = A @ B for a torch CUDA tensor B of shape (K, N); returns C (rows, N)."""
+        import torch
+        K, N = B.shape
+        if K != self.info["cols"]:
+            raise ValueError(f"B has {K} rows, A has {self.info['cols']} columns")
+        b_dtype = {torch.float32: F32, torch.float16: F16, torch.bfloat16: BF16}[B.dtype]
+        layout, ldb = _torch_layout(B)
+        if out is None:
+            out = torch.empty((self.info["rows"], N), device=B.device,
+                              dtype=out_dtype if out_dtype is not None else torch.float32)
+        c_dtype = {torch.float32: F32, torch.float16: F16}[out.dtype]
+        ws_bytes = self.workspace_size(form, b_dtype, N)
+        if workspace is None and ws_bytes:
+            workspace = torch.empty(ws_bytes, dtype=torch.uint8, device=B.device)
+        s = stream if stream is not None else torch.cuda.current_stream(B.device).cuda_stream
+        self.spmm_raw(form, B, b_dtype, layout, ldb, out, c_dtype, out.stride(0), N,
+                      workspace, 0 if workspace is None else workspace.numel(), s)
+        return out
+
+    def spmm_host(self, B: np.ndarray, form: int = FORM_F16, out_dtype=np.float32, stream=0) -> np.ndarray:
+        """Host-buffer SpMM (smat_spmm_host): B (K, N) numpy in, C (rows, N) numpy out."""
+        B = np.asarray(B)
+        K, N = B.shape
+        b_dtype = {np.dtype(np.float32): F32, np.dtype(np.float16): F16}[B.dtype]
+        if B.flags.c_contiguous:
+            layout, ldb = ROW_MAJOR, N
+        elif B.flags.f_contiguous:
+            layout, ldb = COL_MAJOR, K
+        else:
+            B = np.ascontiguousarray(B)
+            layout, ldb = ROW_MAJOR, N
+        out = np.empty((self.info["rows"], N), dtype=out_dtype)
+        c_dtype = F32 if out.dtype == np.float32 else F16
+        check(lib().smat_spmm_host(self._h, form, B.ctypes.data, b_dtype, layout, ldb, out.ctypes.data, c_dtype,
+                                   N, N, stream))
+        return out
+
+    def check_device_error(self):
+        check(lib().smat_bcsr_check_device_error(self._h))

@@ -1,0 +1,105 @@
+"""ctypes binding of libsmat (include/smat.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libsmat.so")
+
+SMAT_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "UNSUPPORTED", 3: "CUDA", 4: "NOMEM", 5: "TIMEOUT", 6: "NO_DEVICE"}
+
+F32, F16, BF16, F64, E4M3 = 0, 1, 2, 3, 4
+FORM_F16, FORM_BF16, FORM_FP8, FORM_SPLIT_BF16 = 0, 1, 2, 3
+ROW_MAJOR, COL_MAJOR = 0, 1
+
+
+class SmatError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"smat {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class CsrStruct(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("nnz", C.c_int64),
+                ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p), ("values", C.c_void_p),
+                ("values_dtype", C.c_int32)]
+
+
+class BcsrOpts(C.Structure):
+    _fields_ = [("block_rows", C.c_int32), ("block_cols", C.c_int32), ("forms", C.c_uint32),
+                ("use_24", C.c_int32), ("row_perm", C.c_void_p), ("device", C.c_int32),
+                ("panel_rows", C.c_int32)]
+
+
+class BcsrInfo(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("rows_padded", C.c_int64),
+                ("cols_padded", C.c_int64), ("nnz", C.c_int64), ("nnzb", C.c_int64),
+                ("n_blocks_24", C.c_int64), ("block_rows", C.c_int32), ("block_cols", C.c_int32),
+                ("panel_rows", C.c_int32), ("n_panels", C.c_int32), ("n_union_cols", C.c_int64),
+                ("fill", C.c_double)]
+
+
+class ReorderStats(C.Structure):
+    _fields_ = [("comparisons", C.c_int64), ("merges", C.c_int64)]
+
+
+# every symbol include/smat.h declares, with its ctypes signature
+_SIGS = {
+    "smat_reorder": (C.c_int, [C.POINTER(CsrStruct), C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                               C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(ReorderStats)]),
+    "smat_bcsr_create": (C.c_int, [C.POINTER(CsrStruct), C.POINTER(BcsrOpts), C.POINTER(C.c_void_p)]),
+    "smat_bcsr_destroy": (C.c_int, [C.c_void_p]),
+    "smat_bcsr_get_info": (C.c_int, [C.c_void_p, C.POINTER(BcsrInfo)]),
+    "smat_bcsr_export": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smat_csr_to_bcsr_host": (C.c_int, [C.POINTER(CsrStruct), C.c_int32, C.c_int32, C.c_void_p,
+                                         C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smat_spmm_workspace_size": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
+    "smat_spmm": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                            C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "smat_spmm_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                                 C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
+    "smat_bcsr_check_device_error": (C.c_int, [C.c_void_p]),
+    "smat_last_error": (C.c_char_p, []),
+    "smat_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libsmat.so (building it first if it is missing). Raises if it cannot load."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("smat_build", os.path.join(PKG_ROOT, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build()
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != SMAT_OK:
+        raise SmatError(status, lib().smat_last_error().decode())
+
+
+def ptr(a) -> int:
+    """Address of a numpy array, a torch tensor, or an int."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
