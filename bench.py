@@ -1,0 +1,391 @@
+"""SpMM benchmark on one GB300 (one JSON line on stdout).
+
+Workload (the R-MAT configuration): R-MAT 2^16 x 2^16 (a=0.57, b=c=0.19,
+d=0.05), 2,000,000 distinct entries, rows randomly permuted, FP16 N(0,1)
+values; Jaccard row reordering (Keeper, tau = 0.6, 16-column blocks,
+16-row groups, fixed-size regrouping); 16 x 16 BCSR; 30 % of the nonzero
+blocks rewritten to an exact 2:4 pattern; B 65536 x 128 FP16 U[-1,1] in the
+reference's column-major layout; FP32 accumulation, FP32 C in the original
+row order. All data synthetic and seeded.
+
+A step is one SpMM C = A * B with A (BCSR), B and C resident on the device.
+`value` is useful TFLOP/s (2 * nnz * N / t); `e2e` is the same metric
+through smat_spmm_host with B copied in from pinned host memory and C copied
+back every step. The matrix A (~0.4 GB) is larger than L2 (129 MB), so no
+L2 flush is done between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl smat|reference]
+
+`--impl reference` times the reference's CPU SpMM (CSR::multiply,
+preprocess/src/general/csr.cpp:47-63, restated in oracle/) on the host cores
+on bounded row samples of the same matrix.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sptc-smat_gb300"))
+
+METRIC = "SpMM useful TFLOP/s, chosen form vs plain FP16 BCSR on one GB300 at stated rel err"
+CACHE = os.environ.get("SMAT_CACHE", "/tmp/smat_bench_cache")
+
+WORKLOAD = {
+    "workload": "rmat16_2M_reordered_tau0.6_bcsr16x16_24frac0.3_N128",
+    "generator": "R-MAT 2^16, a=0.57 b=c=0.19 d=0.05, 2.0M unique, rows permuted, FP16 N(0,1)",
+    "reorder": "Keeper (-a 5), tau=0.6, col_block=16, row_block=16, fixed size (-F 1)",
+    "block": [16, 16],
+    "forced_24_fraction": 0.3,
+    "N": 128,
+    "B": "65536x128 FP16 U[-1,1], column-major",
+    "C": "FP32, original row order",
+    "form": "plain FP16 (tcgen05 kind::f16, FP32 accumulate)",
+    "l2": "no flush: A (~0.4 GB) is larger than the 129 MB L2",
+    "step": "pack B into 4 KB tiles + tensor-core SpMM (2 launches)",
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------------------------- workload
+
+def build_matrix():
+    """(A in original row order, perm, nnz) for the R-MAT workload; the reorder is cached on disk."""
+    import smat
+    from smat import generators as G
+
+    t0 = time.time()
+    A0 = G.rmat(16, 2_000_000, seed=3)
+    key = hashlib.sha1(A0.row_ptr.tobytes() + A0.col_idx.tobytes()).hexdigest()[:16]
+    os.makedirs(CACHE, exist_ok=True)
+    pfile = os.path.join(CACHE, f"perm_{key}_t0.6_b16_B16.npy")
+    if os.path.exists(pfile):
+        perm = np.load(pfile)
+    else:
+        r = smat.reorder(A0, tau=0.6, col_block=16, row_block=16, algo=5, force_fixed=True)
+        perm = r.perm
+        np.save(pfile, perm)
+    Ar = A0.permuted(perm)                       # reordered row order
+    Ar = G.force_24(Ar, 0.3, 16, 16, seed=6)     # exact 2:4 in 30 % of the blocks
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(perm.size)
+    A = Ar.permuted(inv)                         # back to the original row order
+    log(f"[bench] matrix ready in {time.time() - t0:.1f}s: nnz={A.nnz}")
+    return A, perm
+
+
+# ---------------------------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------- arms
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the SpMM kernel from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "spmm_tc_rmat16_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def cpu_baseline(A, N, threads=1, budget_s=12.0, max_rows=None):
+    """CSR::multiply (restated, oracle/) over a bounded row sample; returns (useful TFLOP/s, sample text)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+
+    import oracle as O
+    O.lib()
+    rows = A.rows
+    rp = A.row_ptr.astype(np.int64)
+    ci = A.col_idx.astype(np.int64)
+    v = A.values.astype(np.float32)
+    rng = np.random.default_rng(0)
+    Bc = rng.uniform(-1, 1, rows * N).astype(np.float32)
+    Cc = np.zeros(rows * N, np.float32)
+    # calibrate on a small prefix
+    r_cal = min(rows, 256)
+    t = time.perf_counter()
+    O.csr_multiply_f32_range(rows, 0, r_cal, rp, ci, v, Bc, N, Cc)
+    dt = max(time.perf_counter() - t, 1e-6)
+    per_nnz = dt / max(int(rp[r_cal]), 1)
+    target_nnz = budget_s / per_nnz * threads
+    r1 = int(np.searchsorted(rp, target_nnz))
+    r1 = max(1, min(rows, r1 if max_rows is None else min(r1, max_rows)))
+    bounds = np.linspace(0, r1, threads + 1).astype(np.int64)
+    t = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda k: O.csr_multiply_f32_range(rows, int(bounds[k]), int(bounds[k + 1]), rp, ci, v, Bc, N,
+                                                       Cc), range(threads)))
+    dt = time.perf_counter() - t
+    nnz = int(rp[r1])
+    return 2.0 * nnz * N / dt / 1e12, f"rows 0..{r1} of {rows} ({nnz} of {A.nnz} nnz), N={N}, {dt:.2f}s"
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_init(args)
+    if rank != 0:
+        if pg:
+            pg.barrier()
+        return
+    A, _ = build_matrix()
+    N = WORKLOAD["N"]
+    threads = os.cpu_count() or 1
+    vals = []
+    sample = ""
+    for _ in range(args.warmup):
+        cpu_baseline(A, N, threads=threads, budget_s=1.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, sample = cpu_baseline(A, N, threads=threads, budget_s=max(2.0, 60.0 / max(args.steps, 1)))
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": WORKLOAD,
+            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                             "sample": sample + "; reference CSR::multiply loop (csr.cpp:47-63), row ranges on "
+                                                f"{threads} threads"},
+            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+
+
+def run_smat(args):
+    import torch
+
+    import smat
+    world, rank, local, pg = dist_init(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    A, perm = build_matrix()
+    N = WORKLOAD["N"]
+    t0 = time.time()
+    M = smat.Bcsr(A, block=(16, 16), forms=(smat.FORM_F16,), row_perm=perm, device=local)
+    log(f"[bench] BCSR built in {time.time() - t0:.1f}s: {M.info}")
+    info = M.info
+    rng = np.random.default_rng(2)
+    Bh = rng.uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    B = torch.from_numpy(Bh).to(dev).t().contiguous().t()        # column-major (K, N)
+    Cd = torch.empty((A.rows, N), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    ws_bytes = M.workspace_size(smat.FORM_F16, smat.F16, N)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+
+    def step():
+        M.spmm_raw(smat.FORM_F16, B, smat.F16, smat.COL_MAJOR, A.cols, Cd, smat.F32, N, N, ws, ws_bytes, sp)
+
+    # correctness of this exact configuration against an FP64 product (scipy, independent of the oracle)
+    step()
+    torch.cuda.synchronize(dev)
+    M.check_device_error()
+    import scipy.sparse as sps
+    Asp = sps.csr_matrix((A.values.astype(np.float64), A.col_idx, A.row_ptr), shape=(A.rows, A.cols))
+    ref = Asp @ Bh.astype(np.float64)
+    got = Cd.cpu().numpy().astype(np.float64)
+    rel_err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    log(f"[bench] rel Frobenius error vs FP64: {rel_err:.3e}")
+    del ref, got
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms_total = ev0.elapsed_time(ev1)
+    # per-launch durations of the two kernels on the launching stream: the B
+    # packing and the tensor-core contraction (the roofline's kernel)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for a, b, c in evs:
+        a.record(stream)
+        M.pack_b(smat.FORM_F16, B, smat.F16, smat.COL_MAJOR, A.cols, N, ws, ws_bytes, sp)
+        b.record(stream)
+        M.spmm_packed(smat.FORM_F16, ws, N, Cd, smat.F32, N, sp)
+        c.record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    pack_ms = float(np.mean([a.elapsed_time(b) for a, b, c in evs]))
+    kern_ms = float(np.mean([b.elapsed_time(c) for a, b, c in evs]))
+    ms = ms_total / args.steps
+    if pg:
+        import torch.distributed as dist
+        t = torch.tensor([ms, kern_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, kern_ms = float(t[0]), float(t[1])
+
+    # e2e through the host-buffer entry point: pinned B in, C out, every step
+    Bhost = torch.empty((N, A.cols), dtype=torch.float16).pin_memory()
+    Bhost.copy_(torch.from_numpy(np.ascontiguousarray(Bh.T)))
+    Chost = torch.empty((A.rows, N), dtype=torch.float32).pin_memory()
+    bview = Bhost.numpy().T                                           # (K, N), Fortran order
+    cview = Chost.numpy()
+
+    def step_host():
+        M.spmm_host(bview, smat.FORM_F16, np.float32, out=cview, stream=sp)
+
+    for _ in range(2):
+        step_host()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_host()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if pg:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t[0])
+
+    nnz, nnzb = A.nnz, info["nnzb"]
+    useful = 2.0 * nnz * N
+    stored = 2.0 * nnzb * 256 * N
+    value = world * useful / (ms * 1e-3) / 1e12
+    nbr = info["rows_padded"] // 16
+    # contraction kernel: A blocks (FP16) + 1 metadata byte per block + panel table + packed B once + C (FP32)
+    alg_bytes = nnzb * 256 * 2 + nnzb + 32 * info["n_panels"] + A.cols * N * 2 + A.rows * N * 4
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    tr = profile_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+        "config": dict(WORKLOAD, nnz=nnz, nnzb=nnzb, fill=info["fill"], n_union_cols=info["n_union_cols"],
+                       panel_rows=info["panel_rows"], parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "rel_err_vs_fp64": rel_err,
+        "stored_tflops": world * stored / (ms * 1e-3) / 1e12,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "traffic": (tr["dram_bytes_per_launch"] if tr else None),
+                     "traffic_source": (tr["source"] if tr else None),
+                     "algorithmic_bytes_per_launch": alg_bytes, "kernel": "spmm_tc_kernel",
+                     "kernel_ms": kern_ms, "pack_b_ms": pack_ms},
+        "clocks": clk,
+        "e2e": {"value": world * useful / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                "h2d_bytes_per_step": A.cols * N * 2, "d2h_bytes_per_step": A.rows * N * 4, "ms_per_step": e2e_ms},
+        "gpu_launches": 2 * args.steps,
+    }
+    if rank == 0:
+        cpu_v, sample = cpu_baseline(A, N, threads=1, budget_s=12.0)
+        line["cpu_baseline"] = {"value": cpu_v, "unit": "TFLOP/s", "cores": 1, "kind": "port",
+                                "sample": sample + "; CSR::multiply loop (csr.cpp:47-63), 1 thread"}
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+    M.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="smat", choices=["smat", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_smat(args)
+
+
+if __name__ == "__main__":
+    main()

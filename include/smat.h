@@ -143,8 +143,8 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
 
 /* ---------------------------------------------------------------- step 3 */
 
-/* Bytes of device scratch smat_spmm needs for this form / B dtype / N
- * (0 when B is used in place). */
+/* Bytes of device scratch smat_spmm needs for this form / B dtype / N (the
+ * packed copy of B; twice that for the split form). */
 smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
                                      size_t* bytes);
 
@@ -154,13 +154,24 @@ smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b
  *  B (device): K x N, K = A's column count; element (k, n) at
  *     B[k + n*ldb] (SMAT_COL_MAJOR, the reference layout) or
  *     B[k*ldb + n] (SMAT_ROW_MAJOR). b_dtype: F16 for SMAT_FORM_F16, BF16 for
- *     SMAT_FORM_BF16, or F32 for any form (converted on the fly into workspace).
+ *     SMAT_FORM_BF16, or F32 for any form; it is packed into workspace first.
  *  C (device): rows x N, row-major, C[i*ldc + n], c_dtype F32 or F16; rows
  *     in the ORIGINAL order when the handle was built with row_perm.
  *  workspace (device): smat_spmm_workspace_size() bytes, 256-byte aligned. */
 smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
                       int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
                       int64_t N, void* workspace, size_t workspace_bytes, void* stream);
+
+/* The two halves of smat_spmm, for callers that reuse one B with several
+ * matrices or want to time the contraction alone: smat_spmm_pack_b writes B
+ * into `workspace` in the tensor-core tile layout (4 KB tiles of 16 rows x
+ * 128 columns, 32-byte swizzled; hi and lo halves for the split form);
+ * smat_spmm_packed runs the contraction from that packed copy. */
+smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                             int32_t b_layout, int64_t ldb, int64_t N, void* workspace,
+                             size_t workspace_bytes, void* stream);
+smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packed_b, int64_t N,
+                             void* C, int32_t c_dtype, int64_t ldc, void* stream);
 
 /* Host-buffer variant: copies B (host) in, runs smat_spmm, copies C (host)
  * out, and waits for completion. Uses device buffers cached in the handle. */

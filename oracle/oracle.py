@@ -64,6 +64,9 @@ def lib():
         L.orc_spmm_f64.restype = None
         L.orc_spmm_f64.argtypes = [C.c_int64, C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, C.c_int64,
                                    _f64p, C.c_int64, C.c_int64]
+        L.orc_csr_multiply_f32_range.restype = None
+        L.orc_csr_multiply_f32_range.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                 C.c_void_p, C.c_int64, C.c_void_p]
         L.orc_csr_multiply_f32.restype = None
         L.orc_csr_multiply_f32.argtypes = [C.c_int64, _i64p, _i64p, _f32p, _f32p, C.c_int64, _f32p]
         _lib = L
@@ -249,3 +252,9 @@ def ref_csr_multiply(rowptr, colidx, val, n_cols, B_colmajor, b_cols, rows):
 def is_block_24(blk):
     b = np.ascontiguousarray(np.asarray(blk, np.float16).view(np.uint16))
     return bool(lib().orc_is_block_24(b, b.shape[0], b.shape[1]))
+
+
+def csr_multiply_f32_range(ld, r0, r1, rowptr, colidx, val, B_colmajor, b_cols, C_colmajor):
+    """CSR::multiply's loop over rows [r0, r1); arrays must stay alive (raw pointers)."""
+    lib().orc_csr_multiply_f32_range(ld, r0, r1, rowptr.ctypes.data, colidx.ctypes.data, val.ctypes.data,
+                                     B_colmajor.ctypes.data, b_cols, C_colmajor.ctypes.data)

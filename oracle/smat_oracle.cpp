@@ -315,4 +315,19 @@ void orc_csr_multiply_f32(int64_t rows, const int64_t* rowptr, const int64_t* co
     }
 }
 
+// CSR::multiply's loop (csr.cpp:47-63) restricted to rows [r0, r1) of a
+// matrix whose B and C are column-major with leading dimension `ld`
+// (the full row count, as in the reference). Used to time bounded samples
+// and to split the rows over host threads.
+void orc_csr_multiply_f32_range(int64_t ld, int64_t r0, int64_t r1, const int64_t* rowptr,
+                                const int64_t* colidx, const float* val, const float* B,
+                                int64_t b_cols, float* C) {
+  for (int64_t i = r0; i < r1; i++)
+    for (int64_t nz = rowptr[i]; nz < rowptr[i + 1]; nz++) {
+      int64_t col = colidx[nz];
+      float v = val[nz];
+      for (int64_t j = 0; j < b_cols; j++) C[i + j * ld] += v * B[col + j * ld];
+    }
+}
+
 }  // extern "C"

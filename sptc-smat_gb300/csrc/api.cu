@@ -48,46 +48,6 @@ struct DeviceGuard {
   }
 };
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  });
-  return fn;
-}
-
-// 2-D tiled map over a 16-bit matrix whose rows of `inner` elements are
-// `row_bytes` apart; box = box_inner x box_outer; 32-byte swizzle.
-static smat_status encode_2d_u16(CUtensorMap* tm, CUtensorMapDataType dt, const void* base,
-                                 uint64_t inner, uint64_t outer, uint64_t row_bytes,
-                                 uint32_t box_inner, uint32_t box_outer) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return fail(SMAT_ERR_NO_DEVICE, "cuTensorMapEncodeTiled not available");
-  if ((reinterpret_cast<uintptr_t>(base) & 15) || (row_bytes & 15))
-    return fail(SMAT_ERR_INVALID, "TMA operand must be 16-byte aligned with 16-byte row pitch");
-  if (inner == 0 || outer == 0) return fail(SMAT_ERR_INVALID, "empty TMA operand");
-  cuuint64_t dims[2] = {inner, outer};
-  cuuint64_t strides[1] = {row_bytes};
-  cuuint32_t box[2] = {box_inner, box_outer};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(tm, dt, 2, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
-                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return fail(SMAT_ERR_INVALID, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-  return SMAT_OK;
-}
-
 template <typename T>
 static smat_status upload(T** dptr, const T* src, size_t n) {
   *dptr = nullptr;
@@ -115,14 +75,13 @@ struct smat_bcsr {
   int use24 = 0;
   int64_t n_24 = 0;
   int num_sms = 0;
-  int32_t *d_rowptr = nullptr, *d_row_map = nullptr, *d_ucol_ptr = nullptr, *d_ucol = nullptr,
-          *d_ublk_ptr = nullptr;
-  uint32_t* d_ublk = nullptr;
+  int32_t* d_row_map = nullptr;
+  PanelInfo* d_panels = nullptr;
+  ChunkRec* d_chunks = nullptr;
   Sched sched[3];  // by NSUB (1, 2)
-  uint16_t* d_val[4] = {nullptr, nullptr, nullptr, nullptr};  // F16, BF16, -, SPLIT hi
-  uint16_t* d_val_lo = nullptr;
-  CUtensorMap tm_val[4];
-  CUtensorMap tm_lo;
+  // A blocks in stream order, pre-swizzled, one copy per form: F16, BF16, -, SPLIT hi
+  uint8_t* d_aval[4] = {nullptr, nullptr, nullptr, nullptr};
+  uint8_t* d_aval_lo = nullptr;
   int* d_err = nullptr;
   // smat_spmm_host staging
   std::mutex mu;
@@ -139,8 +98,8 @@ static void free_handle(smat_bcsr* h) {
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
-  void* ptrs[] = {h->d_rowptr, h->d_row_map, h->d_ucol_ptr, h->d_ucol, h->d_ublk_ptr, h->d_ublk,
-                  h->d_val[0], h->d_val[1], h->d_val[2], h->d_val[3], h->d_val_lo, h->d_err,
+  void* ptrs[] = {h->d_row_map, h->d_chunks, h->d_panels,
+                  h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_aval_lo, h->d_err,
                   h->d_bstage, h->d_cstage, h->d_ws, h->sched[1].d_cta_ptr, h->sched[1].d_cta_items,
                   h->sched[2].d_cta_ptr, h->sched[2].d_cta_items};
   for (void* p : ptrs)
@@ -150,7 +109,7 @@ static void free_handle(smat_bcsr* h) {
 }
 
 static int pick_nsub(const smat_bcsr* h, int64_t N, bool split) {
-  if (N > 128 && tc_variant_supported(h->host.bh, h->plan.R, 2, split)) return 2;
+  if (N > 128 && !split && tc_variant_supported(h->host.bh, h->plan.R, 2, split)) return 2;
   return 1;
 }
 
@@ -251,31 +210,28 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
   } while (0)
 
   const HostBcsr& b = h->host;
-  SMAT_TRY(upload(&h->d_rowptr, b.rowptr.data(), b.rowptr.size()));
+  const Plan& pl = h->plan;
   SMAT_TRY(upload(&h->d_row_map, b.row_map.data(), b.row_map.size()));
-  SMAT_TRY(upload(&h->d_ucol_ptr, h->plan.ucol_ptr.data(), h->plan.ucol_ptr.size()));
-  SMAT_TRY(upload(&h->d_ucol, h->plan.ucol.data(), h->plan.ucol.size()));
-  SMAT_TRY(upload(&h->d_ublk_ptr, h->plan.ublk_ptr.data(), h->plan.ublk_ptr.size()));
-  SMAT_TRY(upload(&h->d_ublk, h->plan.ublk.data(), h->plan.ublk.size()));
+  SMAT_TRY(upload(&h->d_chunks, pl.chunks.data(), pl.chunks.size()));
+  SMAT_TRY(upload(&h->d_panels, pl.panels.data(), pl.panels.size()));
   {
     int zero = 0;
     SMAT_TRY(upload(&h->d_err, &zero, 1));
   }
 
-  // per-panel cost: A bytes + B tile bytes (mostly L2 hits) + C bytes written
-  const int64_t nnzb = b.nnzb();
-  std::vector<double> cost(h->plan.n_panels);
-  for (int32_t p = 0; p < h->plan.n_panels; p++) {
-    double blocks = h->plan.ucol_ptr[p + 1] > h->plan.ucol_ptr[p]
-                        ? (double)(h->plan.ublk_ptr[h->plan.ucol_ptr[p + 1]] - h->plan.ublk_ptr[h->plan.ucol_ptr[p]])
-                        : 0.0;
-    double ucols = h->plan.ucol_ptr[p + 1] - h->plan.ucol_ptr[p];
-    cost[p] = blocks * bh * 32.0 + ucols * 128 * 32 * 0.5 + (double)R * bh * 128 * 4 + 2048;
+  // per-panel cost in units of one block: its blocks, its B tile loads (a
+  // 4 KB tile moves 8x the bytes of a block, mostly from L2) and a fixed
+  // per-item cost for the epilogue (R*bh rows of C)
+  std::vector<double> cost(pl.n_panels);
+  for (int32_t p = 0; p < pl.n_panels; p++) {
+    int64_t tiles = 0;
+    for (int32_t c = 0; c < pl.panels[p].nchunks; c++) tiles += pl.chunks[pl.panels[p].chunk_off + c].ntiles;
+    cost[p] = pl.panels[p].nblk + 2.0 * tiles + 0.5 * R * bh;
   }
   for (int nsub = 1; nsub <= 2; nsub++) {
     if (!tc_variant_supported(bh, R, nsub, false)) continue;
     int per_sm = tc_ctas_per_sm(bh, R, nsub, false);
-    int workers = std::max(1, std::min(h->plan.n_panels, h->num_sms * per_sm));
+    int workers = std::max(1, std::min(pl.n_panels, h->num_sms * per_sm));
     std::vector<int32_t> cta_ptr, cta_items;
     assign_items(cost, workers, cta_ptr, cta_items);
     h->sched[nsub].grid = workers;
@@ -283,13 +239,27 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
     SMAT_TRY(upload(&h->sched[nsub].d_cta_items, cta_items.data(), cta_items.size()));
   }
 
-  // values, one device copy per requested form
-  const size_t nval = (size_t)nnzb * bh * bw;
-  const uint64_t rows_of_blocks = (uint64_t)std::max<int64_t>(nnzb, 1) * bh;
+  // A values, one device copy per requested form, in stream order and in the
+  // 32-byte-swizzled shared-memory layout: inside each 256-byte group of 8
+  // rows (32 bytes per row), the two 16-byte halves of rows 4..7 are swapped.
+  const int64_t nnzb = b.nnzb();
+  const size_t bsz = (size_t)bh * bw, ablk = (size_t)bh * 32;
+  auto stream_layout = [&](const std::vector<uint16_t>& vals, std::vector<uint8_t>& out) {
+    out.assign(std::max<size_t>(nnzb, 1) * ablk, 0);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nnzb; k++) {
+      const uint8_t* src = reinterpret_cast<const uint8_t*>(vals.data() + (size_t)pl.stream_blk[k] * bsz);
+      uint8_t* dst = out.data() + (size_t)k * ablk;
+      for (int r = 0; r < bh; r++)
+        for (int c = 0; c < 2; c++)
+          std::memcpy(dst + r * 32 + ((c ^ ((r >> 2) & 1)) * 16), src + r * 32 + c * 16, 16);
+    }
+  };
+  std::vector<uint8_t> lay;
+  const size_t nval = (size_t)nnzb * bsz;
   if (forms & (1u << SMAT_FORM_F16)) {
-    SMAT_TRY(upload(&h->d_val[SMAT_FORM_F16], b.val_f16.data(), nval));
-    SMAT_TRY(encode_2d_u16(&h->tm_val[SMAT_FORM_F16], CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                           h->d_val[SMAT_FORM_F16], 16, rows_of_blocks, 32, 16, bh));
+    stream_layout(b.val_f16, lay);
+    SMAT_TRY(upload(&h->d_aval[SMAT_FORM_F16], lay.data(), lay.size()));
   }
   if (forms & ((1u << SMAT_FORM_BF16) | (1u << SMAT_FORM_SPLIT_BF16))) {
     std::vector<uint16_t> hi(nval), lo(nval);
@@ -297,18 +267,12 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
       hi[i] = f32_to_bf16_bits(b.val[i]);
       lo[i] = f32_to_bf16_bits(b.val[i] - bf16_bits_to_f32(hi[i]));
     }
-    if (forms & (1u << SMAT_FORM_BF16)) {
-      SMAT_TRY(upload(&h->d_val[SMAT_FORM_BF16], hi.data(), nval));
-      SMAT_TRY(encode_2d_u16(&h->tm_val[SMAT_FORM_BF16], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
-                             h->d_val[SMAT_FORM_BF16], 16, rows_of_blocks, 32, 16, bh));
-    }
+    stream_layout(hi, lay);
+    if (forms & (1u << SMAT_FORM_BF16)) SMAT_TRY(upload(&h->d_aval[SMAT_FORM_BF16], lay.data(), lay.size()));
     if (forms & (1u << SMAT_FORM_SPLIT_BF16)) {
-      SMAT_TRY(upload(&h->d_val[SMAT_FORM_SPLIT_BF16], hi.data(), nval));
-      SMAT_TRY(upload(&h->d_val_lo, lo.data(), nval));
-      SMAT_TRY(encode_2d_u16(&h->tm_val[SMAT_FORM_SPLIT_BF16], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
-                             h->d_val[SMAT_FORM_SPLIT_BF16], 16, rows_of_blocks, 32, 16, bh));
-      SMAT_TRY(encode_2d_u16(&h->tm_lo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, h->d_val_lo, 16,
-                             rows_of_blocks, 32, 16, bh));
+      SMAT_TRY(upload(&h->d_aval[SMAT_FORM_SPLIT_BF16], lay.data(), lay.size()));
+      stream_layout(lo, lay);
+      SMAT_TRY(upload(&h->d_aval_lo, lay.data(), lay.size()));
     }
   }
   // keep the FP16 values for export; the FP32 copy is no longer needed
@@ -337,7 +301,11 @@ smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info) {
   info->block_cols = b.bw;
   info->panel_rows = A->plan.R;
   info->n_panels = A->plan.n_panels;
-  info->n_union_cols = (int64_t)A->plan.ucol.size();
+  {
+    int64_t u = 0;
+    for (const auto& p : A->plan.panels) u += p.nucol;
+    info->n_union_cols = u;
+  }
   info->fill = b.nnzb() ? (double)b.nnz / ((double)b.nnzb() * b.bh * b.bw) : 0.0;
   return SMAT_OK;
 }
@@ -368,85 +336,81 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
   return SMAT_OK;
 }
 
-static bool b_in_place(int32_t form, int32_t b_dtype, int32_t b_layout, const void* B, int64_t ldb) {
-  const bool dt_ok = (form == SMAT_FORM_F16 && b_dtype == SMAT_F16) ||
-                     (form == SMAT_FORM_BF16 && b_dtype == SMAT_BF16);
-  return dt_ok && b_layout == SMAT_COL_MAJOR && (ldb % 8) == 0 &&
-         (reinterpret_cast<uintptr_t>(B) & 15) == 0;
-}
-
 smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
                                      size_t* bytes) {
   if (!A || !bytes) return fail(SMAT_ERR_INVALID, "null argument");
-  const int64_t ldo = (A->host.cols_p + 7) / 8 * 8;
-  const size_t one = ((size_t)ldo * (size_t)std::max<int64_t>(N, 1) * 2 + 255) / 256 * 256;
   (void)b_dtype;
+  const size_t one = (packed_b_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
   *bytes = (form == SMAT_FORM_SPLIT_BF16) ? 2 * one : one;
   return SMAT_OK;
 }
 
-smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
-                      int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
-                      int64_t N, void* workspace, size_t workspace_bytes, void* stream_) {
-  if (!A || !B || !C) return fail(SMAT_ERR_INVALID, "null argument");
+static smat_status check_common(const smat_bcsr* A, int32_t form, int64_t N) {
+  if (!A) return fail(SMAT_ERR_INVALID, "null handle");
   if (form < 0 || form > 3 || !(A->forms & (1u << form)))
     return fail(SMAT_ERR_INVALID, "form was not materialised when the handle was built");
   if (form == SMAT_FORM_FP8) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
   if (N <= 0 || N > (1 << 30)) return fail(SMAT_ERR_INVALID, "bad N");
-  if (c_dtype != SMAT_F32 && c_dtype != SMAT_F16) return fail(SMAT_ERR_INVALID, "C must be F32 or F16");
-  if (ldc < N) return fail(SMAT_ERR_INVALID, "ldc < N");
+  return SMAT_OK;
+}
+
+smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                             int32_t b_layout, int64_t ldb, int64_t N, void* workspace,
+                             size_t workspace_bytes, void* stream_) {
+  smat_status st = check_common(A, form, N);
+  if (st != SMAT_OK) return st;
+  if (!B) return fail(SMAT_ERR_INVALID, "null B");
   if (b_layout != SMAT_ROW_MAJOR && b_layout != SMAT_COL_MAJOR) return fail(SMAT_ERR_INVALID, "bad B layout");
   if (b_dtype != SMAT_F32 && b_dtype != SMAT_F16 && b_dtype != SMAT_BF16)
     return fail(SMAT_ERR_INVALID, "B must be F32, F16 or BF16");
-  const HostBcsr& hb = A->host;
-  const int64_t K = hb.cols;
+  const int64_t K = A->host.cols;
   if (b_layout == SMAT_COL_MAJOR ? ldb < K : ldb < N) return fail(SMAT_ERR_INVALID, "ldb too small");
-  cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+  size_t need = 0;
+  smat_spmm_workspace_size(A, form, b_dtype, N, &need);
+  if (!workspace || workspace_bytes < need)
+    return fail(SMAT_ERR_INVALID, "workspace too small (see smat_spmm_workspace_size)");
+  if (reinterpret_cast<uintptr_t>(workspace) & 255) return fail(SMAT_ERR_INVALID, "workspace must be 256-byte aligned");
   DeviceGuard guard(A->device);
   if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+  const bool split = form == SMAT_FORM_SPLIT_BF16;
+  uint8_t* hi = static_cast<uint8_t*>(workspace);
+  uint8_t* lo = split ? hi + need / 2 : nullptr;
+  const int in_dt = b_dtype == SMAT_F32 ? 0 : (b_dtype == SMAT_F16 ? 1 : 2);
+  const int mode = form == SMAT_FORM_F16 ? 0 : (split ? 2 : 1);
+  cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, hi, lo, K, N,
+                         static_cast<cudaStream_t>(stream_));
+  if (e != cudaSuccess) return cuda_fail(e, "pack_b");
+  return SMAT_OK;
+}
 
+smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packed_b, int64_t N,
+                             void* C, int32_t c_dtype, int64_t ldc, void* stream_) {
+  smat_status st = check_common(A, form, N);
+  if (st != SMAT_OK) return st;
+  if (!packed_b || !C) return fail(SMAT_ERR_INVALID, "null argument");
+  if (c_dtype != SMAT_F32 && c_dtype != SMAT_F16) return fail(SMAT_ERR_INVALID, "C must be F32 or F16");
+  if (ldc < N) return fail(SMAT_ERR_INVALID, "ldc < N");
+  const HostBcsr& hb = A->host;
+  if (hb.rows == 0) return SMAT_OK;
+  DeviceGuard guard(A->device);
+  if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
   const bool split = form == SMAT_FORM_SPLIT_BF16;
   const int nsub = pick_nsub(A, N, split);
   const int bh = hb.bh, R = A->plan.R;
   if (!tc_variant_supported(bh, R, nsub, split)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
   const Sched& sc = A->sched[nsub];
-
+  size_t need = 0;
+  smat_spmm_workspace_size(A, form, SMAT_F16, N, &need);
   SpmmArgs args;
   std::memset(&args, 0, sizeof(args));
-  const CUtensorMapDataType bdt =
-      (form == SMAT_FORM_F16) ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   const uint32_t BN = 128u * nsub;
-  const void* Bdev = B;
-  int64_t ldo = ldb;
-  if (!b_in_place(form, b_dtype, b_layout, B, ldb)) {
-    size_t need = 0;
-    smat_spmm_workspace_size(A, form, b_dtype, N, &need);
-    if (!workspace || workspace_bytes < need)
-      return fail(SMAT_ERR_INVALID, "workspace too small (see smat_spmm_workspace_size)");
-    if (reinterpret_cast<uintptr_t>(workspace) & 255) return fail(SMAT_ERR_INVALID, "workspace must be 256-byte aligned");
-    ldo = (hb.cols_p + 7) / 8 * 8;
-    uint16_t* hi = static_cast<uint16_t*>(workspace);
-    uint16_t* lo = split ? hi + need / 4 : nullptr;
-    const int in_dt = b_dtype == SMAT_F32 ? 0 : (b_dtype == SMAT_F16 ? 1 : 2);
-    const int mode = form == SMAT_FORM_F16 ? 0 : (split ? 2 : 1);
-    cudaError_t e = convert_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, hi, lo, ldo,
-                              K, N, stream);
-    if (e != cudaSuccess) return cuda_fail(e, "convert_b");
-    Bdev = hi;
-    if (split) {
-      smat_status s = encode_2d_u16(&args.tmB2, bdt, lo, (uint64_t)K, (uint64_t)N, (uint64_t)ldo * 2, 16, BN);
-      if (s != SMAT_OK) return s;
-    }
-  }
-  smat_status s = encode_2d_u16(&args.tmB, bdt, Bdev, (uint64_t)K, (uint64_t)N, (uint64_t)ldo * 2, 16, BN);
-  if (s != SMAT_OK) return s;
-  args.tmA = A->tm_val[form];
-  if (split) args.tmA2 = A->tm_lo;
-  args.rowptr = A->d_rowptr;
-  args.ucol_ptr = A->d_ucol_ptr;
-  args.ucol = A->d_ucol;
-  args.ublk_ptr = A->d_ublk_ptr;
-  args.ublk = A->d_ublk;
+  args.bpack = static_cast<const uint8_t*>(packed_b);
+  args.bpack2 = split ? args.bpack + need / 2 : nullptr;
+  args.bp_ntiles = packed_b_tiles(N);
+  args.aval = A->d_aval[form];
+  if (split) args.aval2 = A->d_aval_lo;
+  args.panels = A->d_panels;
+  args.chunks = A->d_chunks;
   args.cta_ptr = sc.d_cta_ptr;
   args.cta_items = sc.d_cta_items;
   args.row_map = A->d_row_map;
@@ -456,24 +420,25 @@ smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b
   args.n_tiles = (int32_t)((N + BN - 1) / BN);
   args.nbr = (int32_t)hb.nbr();
   args.c_f16 = c_dtype == SMAT_F16;
-  args.idesc = (form == SMAT_FORM_F16) ? 0x0u : 0x0u;
-  {
-    const uint32_t fmt = (form == SMAT_FORM_F16) ? 0u : 1u;
-    args.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(bh >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-  }
+  // instruction descriptor (kind::f16): FP32 accumulator, FP16 (0) or BF16 (1)
+  // operands, both K-major, M = 128; the kernel adds N per MMA group
+  const uint32_t fmt = (form == SMAT_FORM_F16) ? 0u : 1u;
+  args.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(128 >> 4) << 24);
   args.err = A->d_err;
-  if (A->plan.n_panels == 0 || hb.rows == 0) {
-    // empty matrix: C = 0
-    for (int64_t i = 0; i < hb.rows; i++) {
-      cudaError_t e = cudaMemsetAsync(static_cast<char*>(C) + i * ldc * (c_dtype == SMAT_F16 ? 2 : 4), 0,
-                                      N * (c_dtype == SMAT_F16 ? 2 : 4), stream);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
-    }
-    return SMAT_OK;
-  }
-  cudaError_t e = tc_launch(bh, R, nsub, split, args, sc.grid, stream);
+  cudaError_t e = tc_launch(bh, R, nsub, split, args, sc.grid, static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "spmm kernel launch");
   return SMAT_OK;
+}
+
+smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                      int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
+                      int64_t N, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!A || !B || !C) return fail(SMAT_ERR_INVALID, "null argument");
+  if (c_dtype != SMAT_F32 && c_dtype != SMAT_F16) return fail(SMAT_ERR_INVALID, "C must be F32 or F16");
+  if (ldc < N) return fail(SMAT_ERR_INVALID, "ldc < N");
+  smat_status st = smat_spmm_pack_b(A, form, B, b_dtype, b_layout, ldb, N, workspace, workspace_bytes, stream);
+  if (st != SMAT_OK) return st;
+  return smat_spmm_packed(A, form, workspace, N, C, c_dtype, ldc, stream);
 }
 
 smat_status smat_spmm_host(const smat_bcsr* A_, int32_t form, const void* B_host, int32_t b_dtype,

@@ -165,61 +165,123 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
   plan.R = R;
   plan.n_panels = (int32_t)((nbr + R - 1) / R);
   const int32_t P = plan.n_panels;
-  std::vector<int64_t> ucnt(P + 1, 0), bcnt(P + 1, 0);
-  // pass 1: union sizes
+  if (b.nnzb() >= ((int64_t)1 << 31) - 1) return fail(SMAT_ERR_UNSUPPORTED, "too many blocks");
+  // MMA-issuing warp owning a slot: kMmaWarps equal ranges of slots
+  auto owner = [R](uint32_t slot) -> uint32_t { return (uint32_t)((slot * kMmaWarps) / (uint32_t)R); };
+  struct Local {
+    std::vector<ChunkRec> chunks;
+    std::vector<int32_t> blk;
+    PanelInfo info{};
+    int64_t groups = 0, tiles = 0;
+  };
+  std::vector<Local> loc(P);
 #pragma omp parallel
   {
-    std::vector<int32_t> cols;
+    std::vector<std::pair<int64_t, int32_t>> ent;  // (col * 32 + slot, block)
 #pragma omp for schedule(dynamic, 16)
     for (int32_t p = 0; p < P; p++) {
-      cols.clear();
-      const int64_t br0 = (int64_t)p * R, br1 = std::min<int64_t>(nbr, br0 + R);
-      for (int64_t br = br0; br < br1; br++)
-        for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) cols.push_back(b.colidx[k]);
-      std::sort(cols.begin(), cols.end());
-      ucnt[p + 1] = std::unique(cols.begin(), cols.end()) - cols.begin();
-      bcnt[p + 1] = b.rowptr[br1] - b.rowptr[br0];
-    }
-  }
-  for (int32_t p = 0; p < P; p++) {
-    ucnt[p + 1] += ucnt[p];
-    bcnt[p + 1] += bcnt[p];
-  }
-  if (b.nnzb() >= (int64_t)1 << 27) return fail(SMAT_ERR_UNSUPPORTED, "more than 2^27 blocks");
-  plan.ucol_ptr.resize(P + 1);
-  for (int32_t p = 0; p <= P; p++) plan.ucol_ptr[p] = (int32_t)ucnt[p];
-  plan.ucol.resize(ucnt[P]);
-  plan.ublk_ptr.resize(ucnt[P] + 1);
-  plan.ublk.resize(bcnt[P]);
-  plan.panel_cost.resize(P);
-  // pass 2: per panel, blocks ordered by (column, slot)
-#pragma omp parallel
-  {
-    std::vector<std::pair<int64_t, uint32_t>> ent;  // key = col * 32 + slot
-#pragma omp for schedule(dynamic, 16)
-    for (int32_t p = 0; p < P; p++) {
+      Local& L = loc[p];
       ent.clear();
       const int64_t br0 = (int64_t)p * R, br1 = std::min<int64_t>(nbr, br0 + R);
-      for (int64_t br = br0; br < br1; br++)
+      uint32_t mask = 0;
+      for (int64_t br = br0; br < br1; br++) {
+        if (b.rowptr[br + 1] > b.rowptr[br]) mask |= 1u << (br - br0);
         for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++)
-          ent.push_back({(int64_t)b.colidx[k] * 32 + (br - br0), ((uint32_t)k << 5) | (uint32_t)(br - br0)});
-      std::sort(ent.begin(), ent.end());
-      int64_t u = ucnt[p], e = bcnt[p];
-      int64_t last_col = -1;
-      for (auto& x : ent) {
-        int64_t col = x.first / 32;
-        if (col != last_col) {
-          plan.ucol[u] = (int32_t)col;
-          plan.ublk_ptr[u] = (int32_t)e;
-          u++;
-          last_col = col;
-        }
-        plan.ublk[e++] = x.second;
+          ent.push_back({(int64_t)b.colidx[k] * 32 + (br - br0), k});
       }
-      plan.panel_cost[p] = 0;  // filled by the launcher for its tile width
+      std::sort(ent.begin(), ent.end());
+      L.info.nblk = (int32_t)ent.size();
+      L.info.slot_mask = mask;
+      // accumulate flags in stream order
+      std::vector<uint16_t> acc(ent.size(), 0);
+      uint32_t touched = 0;
+      for (size_t t = 0; t < ent.size(); t++) {
+        const uint32_t slot = (uint32_t)(ent[t].first % 32);
+        if ((touched >> slot) & 1u) acc[t] = kMetaAcc;
+        touched |= 1u << slot;
+      }
+      // chunks: whole union columns where they fit
+      size_t t = 0;
+      int32_t ucols = 0;
+      while (t < ent.size()) {
+        ChunkRec c{};
+        c.nblk = 0;
+        c.ntiles = 0;
+        std::vector<uint16_t> m(kMetaStride, 0);
+        while (t < ent.size()) {
+          const int64_t col = ent[t].first / 32;
+          size_t e = t;
+          while (e < ent.size() && ent[e].first / 32 == col) e++;
+          const int32_t run = (int32_t)(e - t);
+          const int32_t room = kChunkBlocks - c.nblk;
+          if (room == 0) break;
+          if (run > room && c.nblk > 0 && run <= kChunkBlocks) break;  // keep the column whole
+          const int32_t take = std::min(run, room);
+          const int32_t tile = c.ntiles++;
+          c.kb[tile] = (int32_t)(col / 16);
+          if (t == 0 || ent[t - 1].first / 32 != col) ucols++;
+          // MMA groups among the taken blocks
+          for (int32_t g = 0; g < take;) {
+            const uint32_t slot0 = (uint32_t)(ent[t + g].first % 32);
+            int32_t len = 1;
+            while (g + len < take && len < 16) {
+              const uint32_t sl = (uint32_t)(ent[t + g + len].first % 32);
+              if (sl != slot0 + (uint32_t)len) break;
+              if (acc[t + g + len] != acc[t + g]) break;
+              if (owner(sl) != owner(slot0)) break;
+              len++;
+            }
+            for (int32_t q = 0; q < len; q++) {
+              const int32_t pos = c.nblk + g + q;
+              const uint32_t sl = (uint32_t)(ent[t + g + q].first % 32);
+              uint16_t w = (uint16_t)(sl | acc[t + g + q] | (owner(sl) << kMetaOwnerShift) |
+                                      ((uint32_t)tile << kMetaTileShift));
+              if (q == 0) w |= (uint16_t)(len << kMetaLenShift);
+              m[pos] = w;
+            }
+            L.groups++;
+            g += len;
+          }
+          for (int32_t q = 0; q < take; q++) L.blk.push_back(ent[t + q].second);
+          c.nblk += take;
+          t += take;
+        }
+        L.tiles += c.ntiles;
+        for (int q = 0; q < kMetaStride; q++) c.meta[q] = m[q];
+        L.chunks.push_back(c);
+      }
+      L.info.nchunks = (int32_t)L.chunks.size();
+      L.info.nucol = ucols;
     }
   }
-  plan.ublk_ptr[ucnt[P]] = (int32_t)bcnt[P];
+  // concatenate
+  int64_t nch = 0, nb = 0;
+  for (auto& L : loc) {
+    nch += (int64_t)L.chunks.size();
+    nb += (int64_t)L.blk.size();
+  }
+  if (nch >= ((int64_t)1 << 31)) return fail(SMAT_ERR_UNSUPPORTED, "plan too large");
+  plan.panels.resize(P);
+  plan.chunks.resize(nch);
+  plan.stream_blk.resize(nb);
+  plan.n_groups = 0;
+  plan.n_tiles = 0;
+  int64_t co = 0, bo = 0;
+  for (int32_t p = 0; p < P; p++) {
+    Local& L = loc[p];
+    L.info.chunk_off = (int32_t)co;
+    plan.panels[p] = L.info;
+    for (size_t c = 0; c < L.chunks.size(); c++) {
+      ChunkRec r = L.chunks[c];
+      r.blk_off = (int32_t)bo;
+      bo += r.nblk;
+      plan.chunks[co + c] = r;
+    }
+    std::copy(L.blk.begin(), L.blk.end(), plan.stream_blk.begin() + (bo - (int64_t)L.blk.size()));
+    co += (int64_t)L.chunks.size();
+    plan.n_groups += L.groups;
+    plan.n_tiles += L.tiles;
+  }
   return SMAT_OK;
 }
 

@@ -1,10 +1,16 @@
-// convert.cu — prepares the dense operand B for the tensor-core SpMM.
+// convert.cu — packs the dense operand B for the tensor-core SpMM.
 //
-// The SpMM reads B as column-major 16-bit tiles (element (k, n) at
-// B[k + n*ld], the reference's layout, src/cuda_hgemm/src/mma/mmaOBT.cu:75).
-// B given in another dtype or layout is converted here into caller-provided
-// scratch: FP32/FP16/BF16, row- or column-major, to FP16, BF16, or the hi+lo
-// BF16 pair of the split form (hi = bf16(b), lo = bf16(b - hi)).
+// B arrives as FP32, FP16 or BF16, row-major (k*ld + n) or column-major
+// (k + n*ld, the reference's layout, src/cuda_hgemm/src/mma/mmaOBT.cu:75).
+// The SpMM's B producer moves one 16-row slab of a 128-column tile with a
+// single 4 KB bulk copy, so B is first packed into caller-provided scratch:
+// tile (kb, t) holds rows k = 16*kb .. 16*kb+15 and columns
+// n = 128*t .. 128*t+127 as 128 rows (one per n) of 16 16-bit k-values
+// (32 bytes each), in the 32-byte-swizzled shared-memory layout the MMA reads
+// (inside every 8-row group the two 16-byte halves of rows 4..7 are swapped).
+// Tiles are ordered [kb][t]; K is zero-padded to 16 and N to 128 (to 256
+// when there is more than one tile, so that 256-column tiles stay in range).
+// The split form writes hi = bf16(b) and lo = bf16(b - hi) to two buffers.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -33,84 +39,84 @@ __device__ __forceinline__ float load_f<__nv_bfloat16>(const __nv_bfloat16* p) {
   return __bfloat162float(__ldg(p));
 }
 
-template <int OUT>
-__device__ __forceinline__ void store_out(uint16_t* hi, uint16_t* lo, int64_t off, float x) {
-  if (OUT == OUT_F16) {
-    hi[off] = __half_as_ushort(__float2half_rn(x));
-  } else {
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    hi[off] = __bfloat16_as_ushort(h);
-    if (OUT == OUT_SPLIT) lo[off] = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(h)));
-  }
+__device__ __forceinline__ uint4 pack8(const uint16_t* h) {
+  return make_uint4(h[0] | ((uint32_t)h[1] << 16), h[2] | ((uint32_t)h[3] << 16), h[4] | ((uint32_t)h[5] << 16),
+                    h[6] | ((uint32_t)h[7] << 16));
 }
 
-// Column-major input: (k, n) at in[k + n*ldi]. One thread per element, k fastest.
+// One thread per (tile row n, k-block); 128 threads per tile.
 template <typename T, int OUT>
-__global__ void convert_colmajor(const T* __restrict__ in, int64_t ldi, uint16_t* __restrict__ hi,
-                                 uint16_t* __restrict__ lo, int64_t ldo, int64_t K, int64_t N) {
-  const int64_t total = K * N;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t n = i / K, k = i - n * K;
-    store_out<OUT>(hi, lo, k + n * ldo, load_f<T>(in + k + n * ldi));
+__global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ hi,
+                             uint8_t* __restrict__ lo, int64_t K, int64_t N, int ntiles) {
+  const int64_t kb = blockIdx.y;
+  const int t = blockIdx.x;
+  const int r = threadIdx.x;
+  const int64_t n = (int64_t)t * 128 + r;
+  uint16_t h[16], l[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const int64_t k = kb * 16 + i;
+    float x = 0.0f;
+    if (k < K && n < N) x = load_f<T>(layout == 1 ? in + k + n * ldi : in + k * ldi + n);
+    if (OUT == OUT_F16) {
+      h[i] = __half_as_ushort(__float2half_rn(x));
+    } else {
+      const __nv_bfloat16 b = __float2bfloat16_rn(x);
+      h[i] = __bfloat16_as_ushort(b);
+      if (OUT == OUT_SPLIT) l[i] = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(b)));
+    }
   }
-}
-
-// Row-major input: (k, n) at in[k*ldi + n]. 32 x 32 tiles through shared
-// memory so that both the reads (along n) and the writes (along k) coalesce.
-template <typename T, int OUT>
-__global__ void convert_rowmajor(const T* __restrict__ in, int64_t ldi, uint16_t* __restrict__ hi,
-                                 uint16_t* __restrict__ lo, int64_t ldo, int64_t K, int64_t N) {
-  __shared__ float tile[32][33];
-  const int64_t k0 = (int64_t)blockIdx.y * 32, n0 = (int64_t)blockIdx.x * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int r = ty; r < 32; r += 8) {
-    const int64_t k = k0 + r, n = n0 + tx;
-    tile[r][tx] = (k < K && n < N) ? load_f<T>(in + k * ldi + n) : 0.0f;
-  }
-  __syncthreads();
-  for (int c = ty; c < 32; c += 8) {
-    const int64_t n = n0 + c, k = k0 + tx;
-    if (k < K && n < N) store_out<OUT>(hi, lo, k + n * ldo, tile[tx][c]);
+  const int64_t tile = kb * ntiles + t;
+  const int sw = (r >> 2) & 1;
+  uint4* dst = reinterpret_cast<uint4*>(hi + tile * 4096 + r * 32);
+  dst[sw] = pack8(h);
+  dst[sw ^ 1] = pack8(h + 8);
+  if (OUT == OUT_SPLIT) {
+    uint4* d2 = reinterpret_cast<uint4*>(lo + tile * 4096 + r * 32);
+    d2[sw] = pack8(l);
+    d2[sw ^ 1] = pack8(l + 8);
   }
 }
 
 template <typename T, int OUT>
-static cudaError_t run(const void* in, int layout, int64_t ldi, uint16_t* hi, uint16_t* lo,
-                       int64_t ldo, int64_t K, int64_t N, cudaStream_t s) {
-  if (K == 0 || N == 0) return cudaSuccess;
-  if (layout == 1) {
-    const int64_t total = K * N;
-    int64_t blocks = (total + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
-    convert_colmajor<T, OUT><<<(unsigned)blocks, 256, 0, s>>>((const T*)in, ldi, hi, lo, ldo, K, N);
-  } else {
-    dim3 grid((unsigned)((N + 31) / 32), (unsigned)((K + 31) / 32));
-    convert_rowmajor<T, OUT><<<grid, dim3(32, 8), 0, s>>>((const T*)in, ldi, hi, lo, ldo, K, N);
-  }
+static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* hi, uint8_t* lo, int64_t K, int64_t N,
+                            cudaStream_t s) {
+  const int ntiles = (int)packed_b_tiles(N);
+  const int64_t kbs = (K + 15) / 16;
+  if (kbs == 0 || ntiles == 0) return cudaSuccess;
+  dim3 grid((unsigned)ntiles, (unsigned)kbs);
+  pack_b_tiles<T, OUT><<<grid, 128, 0, s>>>((const T*)in, layout, ldi, hi, lo, K, N, ntiles);
   return cudaGetLastError();
 }
 
 }  // namespace dev
 
-cudaError_t convert_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode,
-                      uint16_t* hi, uint16_t* lo, int64_t ldo, int64_t K, int64_t N,
-                      cudaStream_t s) {
+int64_t packed_b_tiles(int64_t N) {
+  const int64_t t = (N + 127) / 128;
+  return t > 1 ? (t + 1) / 2 * 2 : t;
+}
+
+size_t packed_b_bytes(int64_t K, int64_t N) {
+  return (size_t)((K + 15) / 16) * (size_t)packed_b_tiles(N) * 4096;
+}
+
+cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* hi,
+                   uint8_t* lo, int64_t K, int64_t N, cudaStream_t s) {
   using namespace dev;
-#define SMAT_CONV(T)                                                                  \
+#define SMAT_PACK(T)                                                                  \
   switch (out_mode) {                                                                 \
-    case OUT_F16: return run<T, OUT_F16>(in, layout, ldi, hi, lo, ldo, K, N, s);     \
-    case OUT_BF16: return run<T, OUT_BF16>(in, layout, ldi, hi, lo, ldo, K, N, s);   \
-    case OUT_SPLIT: return run<T, OUT_SPLIT>(in, layout, ldi, hi, lo, ldo, K, N, s); \
+    case OUT_F16: return run_pack<T, OUT_F16>(in, layout, ldi, hi, lo, K, N, s);     \
+    case OUT_BF16: return run_pack<T, OUT_BF16>(in, layout, ldi, hi, lo, K, N, s);   \
+    case OUT_SPLIT: return run_pack<T, OUT_SPLIT>(in, layout, ldi, hi, lo, K, N, s); \
     default: return cudaErrorInvalidValue;                                            \
   }
   switch (in_dtype) {
-    case 0: SMAT_CONV(float)
-    case 1: SMAT_CONV(__half)
-    case 2: SMAT_CONV(__nv_bfloat16)
+    case 0: SMAT_PACK(float)
+    case 1: SMAT_PACK(__half)
+    case 2: SMAT_PACK(__nv_bfloat16)
     default: return cudaErrorInvalidValue;
   }
-#undef SMAT_CONV
+#undef SMAT_PACK
 }
 
 }  // namespace smat

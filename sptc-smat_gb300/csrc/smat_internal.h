@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "smat.h"
+#include "spmm_tc.h"
 
 namespace smat {
 
@@ -49,17 +50,19 @@ struct HostBcsr {
 smat_status build_host_bcsr(const smat_csr& A, int32_t bh, int32_t bw, const int64_t* row_perm,
                             HostBcsr& out);
 
-// Work plan of the tensor-core SpMM: panels of `R` block rows; per panel the
-// sorted union of block columns ("union columns"), each with the blocks that
-// use it; per CTA a list of work items (panel, n-tile) balanced by cost.
+// Work plan of the tensor-core SpMM. Panels of `R` block rows; the blocks of
+// a panel are ordered by block column (then block row) and cut into chunks of
+// at most kChunkBlocks blocks; each chunk lists the B tiles (block columns)
+// it needs, and each block carries a metadata word (slot, accumulate flag,
+// MMA group, tile index).
 struct Plan {
   int32_t R = 8;
   int32_t n_panels = 0;
-  std::vector<int32_t> ucol_ptr;     // n_panels + 1
-  std::vector<int32_t> ucol;         // column start of each union column
-  std::vector<int32_t> ublk_ptr;     // n_ucols + 1
-  std::vector<uint32_t> ublk;        // (block index << 5) | slot
-  std::vector<double> panel_cost;    // relative cost of one (panel, n-tile) item
+  std::vector<PanelInfo> panels;
+  std::vector<ChunkRec> chunks;
+  std::vector<int32_t> stream_blk;   // BCSR block index at each stream position
+  int64_t n_groups = 0;              // MMA instructions per pass over A
+  int64_t n_tiles = 0;               // B tile loads per pass over A
 };
 
 smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);

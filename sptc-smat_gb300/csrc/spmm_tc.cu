@@ -11,22 +11,33 @@
 // K = 16 = bw), accumulating in FP32 in tensor memory: R*NSUB accumulators of
 // 128 lanes x bh columns per buffer, double buffered.
 //
-// Blocks of a panel are visited in order of their block column (the panel's
-// "union columns"): the B tile of a column is TMA-loaded ONCE and used by
-// every block row of the panel that has a block there. Every A block is read
-// from HBM once per N tile.
+// Blocks of a panel are visited in order of their block column, so that the
+// B tile of a column is loaded once and used by every block row of the panel
+// that has a block there. The A blocks are stored on the device in exactly
+// that visiting order, already in the shared-memory layout the MMA reads
+// (32-byte swizzle). The pipeline moves STAGES: one stage carries a chunk of
+// up to kChunkBlocks A blocks, every packed B tile those blocks need and one
+// metadata word per block, so the whole hand-off between the copy engine
+// and the tensor cores is one full/empty barrier pair per chunk.
 //
-// Roles (192 threads):
-//   warp 0, lane 0  TMA producer: B tiles into an NB-deep ring, A blocks into
-//                   an NA-deep ring, plus a small descriptor per A stage.
-//   warp 1          allocates / frees TMEM; lane 0 issues the MMAs.
-//   warps 2..5      epilogue: tcgen05.ld -> row scatter through row_map ->
+// Roles (512 threads):
+//   warps 8..15     producers: one bulk copy each per stage (a warp keeps
+//                   only about one copy per ~300 cycles in flight): the B
+//                   tiles, the A chunk (warp 15); warp 8 writes the metadata.
+//   warps 0..3      MMA issuers, lane 0 each, one per quarter of the panel's
+//                   block rows (one thread issues at most one tcgen05.mma
+//                   per ~80-150 cycles; four keep the tensor pipe at its
+//                   per-instruction rate); warp 0 also owns TMEM.
+//   warps 4..7      epilogue: tcgen05.ld -> row scatter through row_map ->
 //                   FP32 or FP16 stores of C (coalesced along N).
+//
+// Consecutive block rows with a block at the same column form one MMA
+// (N = bh * run length), so dense panels need far fewer instructions.
 //
 // Every wait is bounded (see tc_ptx.cuh); on a timeout the kernel raises the
 // CTA's abort flag, records the site in the global error word, lets the
-// producer wait for its own copies in flight and the MMA thread for its own
-// MMAs, frees TMEM and returns.
+// producers wait for their own copies in flight and the MMA threads for
+// their own MMAs, frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -44,9 +55,8 @@ enum : int { KIND_PLAIN = 0, KIND_SPLIT = 1 };
 
 // Error sites recorded in the global error word.
 enum : int {
-  ERR_PROD_B = 101,
   ERR_PROD_A = 102,
-  ERR_PROD_END = 103,
+  ERR_PROD_B = 101,
   ERR_MMA_ACC = 201,
   ERR_MMA_A = 202,
   ERR_MMA_B = 203,
@@ -56,22 +66,31 @@ enum : int {
 
 template <int BH, int R, int NSUB, int KIND>
 struct Cfg {
-  static constexpr int BN = 128 * NSUB;                 // C columns per tile
+  static constexpr int BN = 128 * NSUB;                   // C columns per tile
   static constexpr int NOPS = (KIND == KIND_SPLIT) ? 2 : 1;
-  static constexpr int NA = 32;                         // A stages
-  static constexpr int NB = (NSUB * NOPS >= 2) ? 4 : 6; // B stages
-  static constexpr uint32_t A_STAGE = BH * 32 * NOPS;   // bytes
-  static constexpr uint32_t B_STAGE = BN * 32 * NOPS;
-  static constexpr uint32_t ACC_COLS = R * NSUB * BH;   // TMEM columns per buffer
+  static constexpr int CH = kChunkBlocks;
+  static constexpr uint32_t ABLK = BH * 32;               // bytes of one A block
+  static constexpr uint32_t TILE = BN * 32;               // bytes of one B tile
+  static constexpr uint32_t OFF_B = CH * ABLK * NOPS;     // stage: A blocks (hi, lo), B tiles (hi, lo), metadata
+  static constexpr uint32_t OFF_META = OFF_B + CH * TILE * NOPS;
+  static constexpr uint32_t STAGE = (OFF_META + kMetaStride * 2 + 1023) / 1024 * 1024;
+  // one CTA per SM for R >= 16 (TMEM) or wide stages, two below
+  static constexpr uint32_t BUDGET = 200 * 1024;
+  static constexpr int NS_FIT = (int)(BUDGET / STAGE);
+  static constexpr int NS = NS_FIT < 2 ? 2 : (NS_FIT > 8 ? 8 : NS_FIT);  // stages
+  static constexpr uint32_t SUB_COLS = R * BH;            // TMEM columns of one 128-column subtile
+  static constexpr uint32_t ACC_COLS = NSUB * SUB_COLS;   // TMEM columns per buffer
   static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
-  static constexpr uint32_t SMEM_B = NB * B_STAGE;
-  static constexpr uint32_t SMEM_A = NA * A_STAGE;
-  static constexpr uint32_t SMEM_BARS = 8 * (2 * NA + 2 * NB + 5);
-  static constexpr uint32_t SMEM_BYTES = 1024 + SMEM_B + SMEM_A + SMEM_BARS + 4 * NA + 16;
+  static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
+  static constexpr int NPROD = 8;                         // producer warps
+  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA);
+  static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 16;
+  static constexpr int THREADS = 512;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
   static_assert(R <= 32, "slot field is 5 bits");
+  static_assert(CH <= 8 && kMetaStride * 2 == 16, "tile index is 3 bits; metadata is one 16-byte copy");
 };
 
 // Wait used only while draining after an abort: bounded, ignores the flag.
@@ -86,53 +105,46 @@ __device__ __noinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity, int*
   return true;
 }
 
+// Bounded wait with an inlined fast path for phases that already completed.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
+                                           int where) {
+  return mbar_try_wait(bar, parity) || mbar_wait(bar, parity, abort, err, where);
+}
+
+// Warp roles (16 warps): 0..3 MMA issuers (0 also owns TMEM), 4..7
+// epilogue (TMEM lane quadrants 0..3), 8..15 producers.
 template <int BH, int R, int NSUB, int KIND>
-__global__ void __launch_bounds__(192, 1) spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
+__global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
   using C = Cfg<BH, R, NSUB, KIND>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
-  uint8_t* sB = smem;
-  uint8_t* sA = sB + C::SMEM_B;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sA + C::SMEM_A);
-  uint64_t* afull = bars;
-  uint64_t* aempty = afull + C::NA;
-  uint64_t* bfull = aempty + C::NA;
-  uint64_t* bempty = bfull + C::NB;
-  uint64_t* accfull = bempty + C::NB;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::NS * C::STAGE);
+  uint64_t* full = bars;
+  uint64_t* empty = full + C::NS;
+  uint64_t* accfull = empty + C::NS;
   uint64_t* accempty = accfull + 2;
   uint64_t* drainbar = accempty + 2;
-  uint32_t* sdesc = reinterpret_cast<uint32_t*>(drainbar + 1);
-  uint32_t* tmem_slot = sdesc + C::NA;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drainbar + C::NMMA);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < C::NA; i++) {
-      mbar_init(smem_u32(&afull[i]), 1);
-      mbar_init(smem_u32(&aempty[i]), 1);
-    }
-    for (int i = 0; i < C::NB; i++) {
-      mbar_init(smem_u32(&bfull[i]), 1);
-      mbar_init(smem_u32(&bempty[i]), 1);
+    for (int i = 0; i < C::NS; i++) {
+      mbar_init(smem_u32(&full[i]), C::NPROD);
+      mbar_init(smem_u32(&empty[i]), C::NMMA);
     }
     for (int i = 0; i < 2; i++) {
-      mbar_init(smem_u32(&accfull[i]), 1);
+      mbar_init(smem_u32(&accfull[i]), C::NMMA);
       mbar_init(smem_u32(&accempty[i]), 4);
     }
-    mbar_init(smem_u32(drainbar), 1);
+    for (int i = 0; i < C::NMMA; i++) mbar_init(smem_u32(&drainbar[i]), 1);
     *abort_flag = 0;
     fence_barrier_init();
-    prefetch_tensormap(&args.tmA);
-    prefetch_tensormap(&args.tmB);
-    if (KIND == KIND_SPLIT) {
-      prefetch_tensormap(&args.tmA2);
-      prefetch_tensormap(&args.tmB2);
-    }
   }
-  if (warp == 1) {
+  if (warp == 0) {
     tmem_alloc(smem_u32(tmem_slot), C::TMEM_COLS);
     tmem_relinquish();
   }
@@ -145,149 +157,177 @@ __global__ void __launch_bounds__(192, 1) spmm_tc_kernel(const __grid_constant__
   const int it1 = args.cta_ptr[blockIdx.x + 1];
   const int n_tiles = args.n_tiles;
   int* err = args.err;
+  const uint32_t smem0 = smem_u32(smem);
 
-  if (warp == 0) {
-    if (lane == 0) {
-      // ------------------------------------------------------------ producer
-      uint32_t ai = 0, bi = 0;
-      bool ok = true;
-      const uint32_t sA0 = smem_u32(sA), sB0 = smem_u32(sB);
-      for (int it = it0; it < it1 && ok; ++it) {
-        const int panel = args.cta_items[it];
-        const int u0 = args.ucol_ptr[panel], u1 = args.ucol_ptr[panel + 1];
-        for (int nt = 0; nt < n_tiles && ok; ++nt) {
-          const int n0 = nt * C::BN;
-          uint32_t touched = 0;
-          for (int u = u0; u < u1 && ok; ++u) {
-            const int col = args.ucol[u];
-            const uint32_t sb = bi % C::NB;
-            if (!mbar_wait(smem_u32(&bempty[sb]), ((bi / C::NB) & 1) ^ 1, abort_flag, err, ERR_PROD_B)) {
+  if (warp >= 8) {
+    // --------------------------------------------------------------- producers
+    // One warp completes only about one bulk copy at a time (~20 B/cycle), so
+    // the copies of every stage are spread over eight producer warps, and the
+    // duties rotate with the stage number c: producer c % 8 copies the
+    // chunk's A blocks (from HBM, the slowest copy) and writes its metadata,
+    // producer (c + 1 + t) % 8 copies B tile t. Each producer arrives once per
+    // stage with the bytes it issued; the stage completes when all eight have
+    // arrived and every copy landed. Chunk records are read 32 at a time (one
+    // per lane) and each lane pre-selects what its warp needs from its record.
+    const int pw = warp - 8;
+    const uint64_t pol_a = make_l2_policy_evict_first();  // A streams through L2 once
+    const uint64_t pol_b = make_l2_policy_evict_last();   // B tiles are re-read by many CTAs
+    uint32_t ci = 0;
+    bool ok = true;
+    for (int it = it0; it < it1 && ok; ++it) {
+      const PanelInfo pi = args.panels[args.cta_items[it]];
+      for (int nt = 0; nt < n_tiles && ok; ++nt) {
+        for (int base = 0; base < pi.nchunks && ok; base += 32) {
+          const int cnt = min(32, pi.nchunks - base);
+          // this lane's record belongs to stage number ci + lane
+          const uint32_t my_ci = ci + (uint32_t)lane;
+          const int my_tile = (int)((uint32_t)pw - my_ci - 1u) & 7;
+          const bool my_a = (int)(my_ci & 7u) == pw;
+          int4 r0 = make_int4(0, 0, 0, 0), r3 = r0;
+          int mykb = 0;
+          if (lane < cnt) {
+            const int4* rp = reinterpret_cast<const int4*>(args.chunks + pi.chunk_off + base + lane);
+            r0 = rp[0];  // blk_off, nblk, ntiles, -
+            const int4 kbv = rp[1 + (my_tile >> 2)];
+            mykb = (my_tile & 3) == 0 ? kbv.x : (my_tile & 3) == 1 ? kbv.y : (my_tile & 3) == 2 ? kbv.z : kbv.w;
+            if (my_a) r3 = rp[3];  // metadata words
+          }
+          for (int i = 0; i < cnt; ++i, ++ci) {
+            const int blk_off = __shfl_sync(0xffffffffu, r0.x, i);
+            const int nblk = __shfl_sync(0xffffffffu, r0.y, i);
+            const int ntiles = __shfl_sync(0xffffffffu, r0.z, i);
+            const int kb = __shfl_sync(0xffffffffu, mykb, i);
+            int4 mv;
+            mv.x = __shfl_sync(0xffffffffu, r3.x, i);
+            mv.y = __shfl_sync(0xffffffffu, r3.y, i);
+            mv.z = __shfl_sync(0xffffffffu, r3.z, i);
+            mv.w = __shfl_sync(0xffffffffu, r3.w, i);
+            const int tile = (int)((uint32_t)pw - ci - 1u) & 7;
+            const bool do_a = (int)(ci & 7u) == pw;
+            int good = 1;
+            if (lane == 0) {
+              const uint32_t s = ci % C::NS;
+              if (wait_phase(smem_u32(&empty[s]), ((ci / C::NS) & 1) ^ 1, abort_flag, err, ERR_PROD_A)) {
+                const uint32_t st = smem0 + s * C::STAGE;
+                const uint32_t fb = smem_u32(&full[s]);
+                uint32_t bytes = 0;
+                if (tile < ntiles) bytes += C::TILE * C::NOPS;
+                if (do_a) {
+                  bytes += nblk * C::ABLK * C::NOPS;
+                  *reinterpret_cast<int4*>(smem + s * C::STAGE + C::OFF_META) = mv;
+                }
+                mbar_arrive_expect_tx(fb, bytes);
+                if (do_a) {
+                  const size_t aoff = (size_t)blk_off * C::ABLK;
+                  bulk_load_hint(st, args.aval + aoff, nblk * C::ABLK, fb, pol_a);
+                  if (KIND == KIND_SPLIT)
+                    bulk_load_hint(st + C::CH * C::ABLK, args.aval2 + aoff, nblk * C::ABLK, fb, pol_a);
+                }
+                if (tile < ntiles) {
+                  const size_t boff = ((size_t)kb * args.bp_ntiles + (size_t)nt * NSUB) * 4096;
+                  bulk_load_hint(st + C::OFF_B + tile * C::TILE * C::NOPS, args.bpack + boff, C::TILE, fb, pol_b);
+                  if (KIND == KIND_SPLIT)
+                    bulk_load_hint(st + C::OFF_B + tile * C::TILE * C::NOPS + C::TILE, args.bpack2 + boff, C::TILE,
+                                   fb, pol_b);
+                }
+              } else {
+                good = 0;
+              }
+            }
+            good = __shfl_sync(0xffffffffu, good, 0);
+            if (!good) {
               ok = false;
               break;
             }
-            const uint32_t bf = smem_u32(&bfull[sb]);
-            mbar_arrive_expect_tx(bf, C::B_STAGE);
-            tma_load_2d(sB0 + sb * C::B_STAGE, &args.tmB, col, n0, bf);
-            if (KIND == KIND_SPLIT)
-              tma_load_2d(sB0 + sb * C::B_STAGE + C::BN * 32, &args.tmB2, col, n0, bf);
-            ++bi;
-            const int e0 = args.ublk_ptr[u], e1 = args.ublk_ptr[u + 1];
-            for (int e = e0; e < e1; ++e) {
-              const uint32_t v = args.ublk[e];
-              const uint32_t blk = v >> 5, slot = v & 31u;
-              const uint32_t sa = ai % C::NA;
-              if (!mbar_wait(smem_u32(&aempty[sa]), ((ai / C::NA) & 1) ^ 1, abort_flag, err, ERR_PROD_A)) {
-                ok = false;
-                break;
-              }
-              sdesc[sa] = slot | (((touched >> slot) & 1u) << 8) | ((e == e0 ? 1u : 0u) << 9) |
-                          ((e == e1 - 1 ? 1u : 0u) << 10);
-              touched |= 1u << slot;
-              const uint32_t af = smem_u32(&afull[sa]);
-              mbar_arrive_expect_tx(af, C::A_STAGE);
-              tma_load_2d(sA0 + sa * C::A_STAGE, &args.tmA, 0, (int32_t)(blk * BH), af);
-              if (KIND == KIND_SPLIT)
-                tma_load_2d(sA0 + sa * C::A_STAGE + BH * 32, &args.tmA2, 0, (int32_t)(blk * BH), af);
-              ++ai;
-            }
           }
-          if (!ok) break;
-          const uint32_t sa = ai % C::NA;
-          if (!mbar_wait(smem_u32(&aempty[sa]), ((ai / C::NA) & 1) ^ 1, abort_flag, err, ERR_PROD_END)) {
-            ok = false;
-            break;
-          }
-          sdesc[sa] = 1u << 31;  // end of work item
-          mbar_arrive(smem_u32(&afull[sa]));
-          ++ai;
         }
       }
-      if (!ok) {
-        // wait for this thread's own copies still in flight
-        for (uint32_t k = (ai > (uint32_t)C::NA ? ai - C::NA : 0); k < ai; ++k)
-          mbar_wait_drain(smem_u32(&afull[k % C::NA]), (k / C::NA) & 1, err);
-        for (uint32_t k = (bi > (uint32_t)C::NB ? bi - C::NB : 0); k < bi; ++k)
-          mbar_wait_drain(smem_u32(&bfull[k % C::NB]), (k / C::NB) & 1, err);
-      }
     }
-  } else if (warp == 1) {
+    if (!ok && lane == 0) {
+      // wait for this warp's own copies still in flight
+      for (uint32_t k = (ci > (uint32_t)C::NS ? ci - C::NS : 0); k < ci; ++k)
+        mbar_wait_drain(smem_u32(&full[k % C::NS]), (k / C::NS) & 1, err);
+    }
+  } else if (warp < C::NMMA) {
     if (lane == 0) {
-      // ------------------------------------------------------------ MMA issuer
-      const uint32_t idesc = args.idesc;
-      uint32_t ai = 0, bi = 0, k = 0;
+      // ----------------------------------------------------------- MMA issuers
+      // Issuer w owns the groups whose owner field is w (a quarter of the
+      // panel's block rows) and releases every stage once. One thread can
+      // issue a tcgen05.mma only every ~80-150 cycles; four keep the tensor
+      // pipe at its per-instruction rate for these narrow MMAs.
+      const uint32_t mine = (uint32_t)warp;
+      const uint32_t idesc0 = args.idesc;  // without the N field
+      uint32_t ci = 0, k = 0;
       bool ok = true, issued = false;
-      const uint32_t sA0 = smem_u32(sA), sB0 = smem_u32(sB);
       for (int it = it0; it < it1 && ok; ++it) {
+        const int nchunks = args.panels[args.cta_items[it]].nchunks;
         for (int nt = 0; nt < n_tiles && ok; ++nt, ++k) {
           const uint32_t buf = k & 1;
           const uint32_t dbase = tmem + buf * C::ACC_COLS;
-          if (!mbar_wait(smem_u32(&accempty[buf]), ((k >> 1) & 1) ^ 1, abort_flag, err, ERR_MMA_ACC)) {
+          if (!wait_phase(smem_u32(&accempty[buf]), ((k >> 1) & 1) ^ 1, abort_flag, err, ERR_MMA_ACC)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          while (true) {
-            const uint32_t sa = ai % C::NA;
-            if (!mbar_wait(smem_u32(&afull[sa]), (ai / C::NA) & 1, abort_flag, err, ERR_MMA_A)) {
+          for (int c = 0; c < nchunks; ++c, ++ci) {
+            const uint32_t s = ci % C::NS;
+            // the stage's copies landed (complete_tx); the MMA reads shared
+            // memory through the async proxy, so no tcgen05 fence is needed
+            if (!wait_phase(smem_u32(&full[s]), (ci / C::NS) & 1, abort_flag, err, ERR_MMA_A)) {
               ok = false;
               break;
             }
-            const uint32_t d = sdesc[sa];
-            if (d >> 31) {
-              mbar_arrive(smem_u32(&aempty[sa]));
-              ++ai;
-              umma_commit(smem_u32(&accfull[buf]));
-              break;
-            }
-            const uint32_t sb = bi % C::NB;
-            if (d & (1u << 9)) {
-              if (!mbar_wait(smem_u32(&bfull[sb]), (bi / C::NB) & 1, abort_flag, err, ERR_MMA_B)) {
-                ok = false;
-                break;
-              }
-            }
-            tc_fence_after();
-            const uint32_t slot = d & 31u, acc = (d >> 8) & 1u;
-            const uint32_t a_addr = sA0 + sa * C::A_STAGE;
-            const uint32_t b_addr = sB0 + sb * C::B_STAGE;
-            const uint64_t a_hi = desc_kmajor_sw32(a_addr);
+            const uint4 mv = *reinterpret_cast<const uint4*>(smem + s * C::STAGE + C::OFF_META);
+            const uint32_t mw[4] = {mv.x, mv.y, mv.z, mv.w};
+            // descriptors of operands inside the stage = stage descriptor + offset / 16
+            const uint64_t sdesc = desc_kmajor_sw32(smem0 + s * C::STAGE);
 #pragma unroll
-            for (int j = 0; j < NSUB; ++j) {
-              const uint32_t dcol = dbase + slot * (NSUB * BH) + j * BH;
-              const uint64_t b_hi = desc_kmajor_sw32(b_addr + j * 128 * 32);
-              umma_f16(dcol, b_hi, a_hi, idesc, acc);
-              if (KIND == KIND_SPLIT) {
-                const uint64_t a_lo = desc_kmajor_sw32(a_addr + BH * 32);
-                const uint64_t b_lo = desc_kmajor_sw32(b_addr + C::BN * 32 + j * 128 * 32);
-                umma_f16(dcol, b_hi, a_lo, idesc, 1);
-                umma_f16(dcol, b_lo, a_hi, idesc, 1);
+            for (int i = 0; i < C::CH; ++i) {
+              const uint32_t m = (mw[i >> 1] >> ((i & 1) * 16)) & 0xffffu;
+              const uint32_t len = (m >> kMetaLenShift) & 31u;
+              if (len == 0 || ((m >> kMetaOwnerShift) & 3u) != mine) continue;
+              const uint32_t slot = m & 31u, acc = (m >> 5) & 1u;
+              const uint32_t tile = m >> kMetaTileShift;
+              const uint32_t idesc = idesc0 | (((len * BH) >> 3) << 17);
+              const uint64_t a_hi = sdesc + ((i * C::ABLK) >> 4);
+              const uint64_t b_hi0 = sdesc + ((C::OFF_B + tile * C::TILE * C::NOPS) >> 4);
+#pragma unroll
+              for (int j = 0; j < NSUB; ++j) {
+                const uint32_t dcol = dbase + j * C::SUB_COLS + slot * BH;
+                const uint64_t b_hi = b_hi0 + ((j * 128 * 32) >> 4);
+                umma_f16(dcol, b_hi, a_hi, idesc, acc);
+                if (KIND == KIND_SPLIT) {
+                  const uint64_t a_lo = a_hi + ((C::CH * C::ABLK) >> 4);
+                  const uint64_t b_lo = b_hi + (C::TILE >> 4);
+                  umma_f16(dcol, b_hi, a_lo, idesc, 1);
+                  umma_f16(dcol, b_lo, a_hi, idesc, 1);
+                }
               }
+              issued = true;
             }
-            issued = true;
-            umma_commit(smem_u32(&aempty[sa]));
-            if (d & (1u << 10)) {
-              umma_commit(smem_u32(&bempty[sb]));
-              ++bi;
-            }
-            ++ai;
+            umma_commit(smem_u32(&empty[s]));
           }
+          if (!ok) break;
+          umma_commit(smem_u32(&accfull[buf]));
         }
       }
       if (!ok && issued) {
-        umma_commit(smem_u32(drainbar));
-        mbar_wait_drain(smem_u32(drainbar), 0, err);
+        const uint32_t db = smem_u32(&drainbar[warp]);
+        umma_commit(db);
+        mbar_wait_drain(db, 0, err);
       }
     }
-  } else {
+  } else if (warp >= 4) {
     // -------------------------------------------------------------- epilogue
     const uint32_t q = warp & 3;  // TMEM lane quadrant this warp may access
     uint32_t k = 0;
     bool ok = true;
     for (int it = it0; it < it1 && ok; ++it) {
       const int panel = args.cta_items[it];
+      const uint32_t slot_mask = args.panels[panel].slot_mask;
       for (int nt = 0; nt < n_tiles; ++nt, ++k) {
         const uint32_t buf = k & 1;
-        if (!mbar_wait(smem_u32(&accfull[buf]), (k >> 1) & 1, abort_flag, err, ERR_EPI)) {
+        if (!wait_phase(smem_u32(&accfull[buf]), (k >> 1) & 1, abort_flag, err, ERR_EPI)) {
           ok = false;
           break;
         }
@@ -296,7 +336,7 @@ __global__ void __launch_bounds__(192, 1) spmm_tc_kernel(const __grid_constant__
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
           if (rb >= args.nbr) break;
-          const bool empty = args.rowptr[rb + 1] == args.rowptr[rb];
+          const bool empty_slot = ((slot_mask >> s) & 1u) == 0;
           const int myrow = lane < BH ? args.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
@@ -304,8 +344,8 @@ __global__ void __launch_bounds__(192, 1) spmm_tc_kernel(const __grid_constant__
 #pragma unroll
             for (int h = 0; h < BH; h += 16) {
               float v[16];
-              if (!empty) {
-                tmem_ld_x16(dbase + s * (NSUB * BH) + j * BH + h, v);
+              if (!empty_slot) {
+                tmem_ld_x16(dbase + j * C::SUB_COLS + s * BH + h, v);
               } else {
 #pragma unroll
                 for (int m = 0; m < 16; ++m) v[m] = 0.0f;
@@ -333,7 +373,7 @@ __global__ void __launch_bounds__(192, 1) spmm_tc_kernel(const __grid_constant__
 
   tc_fence_before();
   __syncthreads();
-  if (warp == 1) {
+  if (warp == 0) {
     tc_fence_after();
     tmem_dealloc(tmem, C::TMEM_COLS);
   }
@@ -344,18 +384,29 @@ static cudaError_t launch_one(const SpmmArgs& args, int grid, cudaStream_t strea
   using C = Cfg<BH, R, NSUB, KIND>;
   auto kfn = spmm_tc_kernel<BH, R, NSUB, KIND>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
-  if (e != cudaSuccess) return e;
-  kfn<<<grid, 192, C::SMEM_BYTES, stream>>>(args);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // do not leave the error for the next call to find
+    return e;
+  }
+  kfn<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(args);
   return cudaGetLastError();
 }
 
+// Co-resident CTAs per SM: limited by TMEM (512 columns per SM) and by what
+// the occupancy calculator reports for the shared memory and registers.
 template <int BH, int R, int NSUB, int KIND>
 static int ctas_per_sm_one() {
   using C = Cfg<BH, R, NSUB, KIND>;
+  auto kfn = spmm_tc_kernel<BH, R, NSUB, KIND>;
   int by_tmem = 512 / C::TMEM_COLS;
-  int by_smem = (227 * 1024) / (C::SMEM_BYTES + 1024);
-  int n = by_tmem < by_smem ? by_tmem : by_smem;
-  return n < 1 ? 1 : (n > 4 ? 4 : n);
+  int occ = 1;
+  if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, C::THREADS, C::SMEM_BYTES) != cudaSuccess) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  int n = by_tmem < occ ? by_tmem : occ;
+  return n < 1 ? 1 : n;
 }
 
 }  // namespace dev
@@ -372,11 +423,8 @@ static int ctas_per_sm_one() {
   X(16, 4, 1, 1)            \
   X(16, 8, 1, 1)            \
   X(16, 16, 1, 1)           \
-  X(16, 4, 2, 1)            \
-  X(16, 8, 2, 1)            \
   X(32, 4, 1, 1)            \
-  X(32, 8, 1, 1)            \
-  X(32, 4, 2, 1)
+  X(32, 8, 1, 1)
 
 bool tc_variant_supported(int bh, int R, int nsub, bool split) {
 #define SMAT_TC_MATCH(BH, R_, NS, K) \

@@ -202,6 +202,15 @@ class Bcsr:
         check(lib().smat_spmm(self._h, form, ptr(B), b_dtype, b_layout, ldb, ptr(Cmat), c_dtype, ldc, N,
                               ptr(workspace), workspace_bytes, stream))
 
+    def pack_b(self, form, B, b_dtype, b_layout, ldb, N, workspace, workspace_bytes, stream=0):
+        """smat_spmm_pack_b: B into the packed tile layout in `workspace`."""
+        check(lib().smat_spmm_pack_b(self._h, form, ptr(B), b_dtype, b_layout, ldb, N, ptr(workspace),
+                                     workspace_bytes, stream))
+
+    def spmm_packed(self, form, packed_b, N, Cmat, c_dtype, ldc, stream=0):
+        """smat_spmm_packed: the contraction alone, from a packed B."""
+        check(lib().smat_spmm_packed(self._h, form, ptr(packed_b), N, ptr(Cmat), c_dtype, ldc, stream))
+
     def spmm(self, B, form: int = FORM_F16, out=None, out_dtype=None, workspace=None, stream=None):
         """C = A @ B for a torch CUDA tensor B of shape (K, N); returns C (rows, N)."""
         import torch
@@ -222,8 +231,10 @@ class Bcsr:
                       workspace, 0 if workspace is None else workspace.numel(), s)
         return out
 
-    def spmm_host(self, B: np.ndarray, form: int = FORM_F16, out_dtype=np.float32, stream=0) -> np.ndarray:
-        """Host-buffer SpMM (smat_spmm_host): B (K, N) numpy in, C (rows, N) numpy out."""
+    def spmm_host(self, B: np.ndarray, form: int = FORM_F16, out_dtype=np.float32, out=None,
+                  stream=0) -> np.ndarray:
+        """Host-buffer SpMM (smat_spmm_host): B (K, N) numpy in, C (rows, N) numpy out.
+        Pinned host buffers make the copies asynchronous DMA."""
         B = np.asarray(B)
         K, N = B.shape
         b_dtype = {np.dtype(np.float32): F32, np.dtype(np.float16): F16}[B.dtype]
@@ -234,7 +245,10 @@ class Bcsr:
         else:
             B = np.ascontiguousarray(B)
             layout, ldb = ROW_MAJOR, N
-        out = np.empty((self.info["rows"], N), dtype=out_dtype)
+        if out is None:
+            out = np.empty((self.info["rows"], N), dtype=out_dtype)
+        if not out.flags.c_contiguous or out.shape != (self.info["rows"], N):
+            raise ValueError("out must be a C-contiguous (rows, N) array")
         c_dtype = F32 if out.dtype == np.float32 else F16
         check(lib().smat_spmm_host(self._h, form, B.ctypes.data, b_dtype, layout, ldb, out.ctypes.data, c_dtype,
                                    N, N, stream))

@@ -60,6 +60,10 @@ _SIGS = {
     "smat_spmm_workspace_size": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
     "smat_spmm": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                             C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "smat_spmm_pack_b": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64,
+                                   C.c_void_p, C.c_size_t, C.c_void_p]),
+    "smat_spmm_packed": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_int64,
+                                   C.c_void_p]),
     "smat_spmm_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                                  C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
     "smat_bcsr_check_device_error": (C.c_int, [C.c_void_p]),
