@@ -23,7 +23,7 @@ import numpy as np
 from ._lib import (BF16, COL_MAJOR, E4M3, F16, F32, F64, FORM_BF16, FORM_F16, FORM_FP8, FORM_SPLIT_BF16,
                    ROW_MAJOR, BcsrInfo, BcsrOpts, CsrStruct, ReorderStats, SmatError, check, lib, ptr)
 
-__all__ = ["Csr", "Bcsr", "reorder", "csr_to_bcsr_host", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
+__all__ = ["Csr", "Bcsr", "reorder", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
            "FORM_FP8", "FORM_SPLIT_BF16", "F32", "F16", "BF16", "F64", "E4M3", "ROW_MAJOR", "COL_MAJOR"]
 
 _VAL_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float16): F16, np.dtype(np.float64): F64}
@@ -256,3 +256,29 @@ class Bcsr:
 
     def check_device_error(self):
         check(lib().smat_bcsr_check_device_error(self._h))
+
+
+def partition_rows(csr: Csr, world: int, block_rows: int = 16):
+    """1-D partition of the rows into `world` contiguous ranges of whole block
+    rows, balanced by nonzeros: the natural sharding of the SpMM (each shard
+    owns its rows of C; B is replicated; no exchange is needed)."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    nbr = (csr.rows + block_rows - 1) // block_rows
+    ends = np.minimum(np.arange(1, nbr + 1) * block_rows, csr.rows)
+    cum = csr.row_ptr[ends]
+    total = int(csr.row_ptr[-1])
+    cuts = [0]
+    for w in range(1, world):
+        target = total * w / world
+        b = int(np.searchsorted(cum, target, side="left"))
+        cuts.append(max(cuts[-1], min(int(ends[b]) if b < nbr else csr.rows, csr.rows)))
+    cuts.append(csr.rows)
+    return [(cuts[i], cuts[i + 1]) for i in range(world)]
+
+
+def row_slice(csr: Csr, r0: int, r1: int) -> Csr:
+    """Rows [r0, r1) as their own CSR (same columns)."""
+    a, b = int(csr.row_ptr[r0]), int(csr.row_ptr[r1])
+    vals = None if csr.values is None else csr.values[a:b]
+    return Csr(r1 - r0, csr.cols, csr.row_ptr[r0:r1 + 1] - a, csr.col_idx[a:b], vals)

@@ -1,0 +1,156 @@
+"""Generates the golden fixtures in this directory by running the REFERENCE's
+own code (built from its sources by oracle/Makefile into oracle/_ref/):
+
+* golden_preprocess.npz — Jaccard distances and merge_rows results
+  (preprocess/src/general/blocking.cpp, utilities.cpp), and Keeper groupings,
+  permutations and counters (BlockingEngine::GetGrouping with
+  `-a 5 -b b -B B -F f -t tau`) on the reference's TEST matrix, on its
+  bcsstk18_r minitest graph and on seeded random patterns;
+* golden_bcsr.npz — SparseMatrix::csrToBcsr (src/cuda_hgemm/src/common/matrix.h)
+  block structure and values on seeded random CSRs with file-order columns;
+* golden_multiply.npz — CSR::multiply (preprocess/src/general/csr.cpp) on a
+  seeded case.
+
+Run it where the reference sources are present:
+
+    python tests/golden/make_golden.py [--reference /path/to/sptc-smat]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+
+def read_el(path):
+    """Edge list as CSR::read_from_edgelist reads it (rows ascending, `row col [value]`,
+    rows = last row + 1, cols = max column + 1)."""
+    rows, cols, vals = [], [], []
+    with open(path) as f:
+        for line in f:
+            if not line.strip() or line[0] in "#%":
+                continue
+            t = line.split()
+            rows.append(int(t[0]))
+            cols.append(int(t[1]))
+            vals.append(float(t[2]) if len(t) > 2 else 1.0)
+    r = np.array(rows, np.int64)
+    n_rows = int(r[-1]) + 1
+    rp = np.zeros(n_rows + 1, np.int64)
+    np.add.at(rp, r + 1, 1)
+    rp = np.cumsum(rp)
+    return rp, np.array(cols, np.int64), np.array(vals, np.float32), n_rows, int(max(cols)) + 1
+
+
+def rand_pattern(rng, rows, cols, deg, shuffle=False):
+    rp = [0]
+    cs = []
+    for _ in range(rows):
+        c = np.unique(rng.integers(0, cols, int(rng.integers(0, deg))))
+        if shuffle:
+            rng.shuffle(c)
+        cs.extend(c.tolist())
+        rp.append(len(cs))
+    return np.array(rp, np.int64), np.array(cs, np.int64)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    import oracle as O
+    O.build(ref=True)
+    if not O.ref_available():
+        raise SystemExit("reference build not available")
+    rng = np.random.default_rng(20261203)
+    out = {}
+
+    # --- Jaccard / merge_rows
+    a = np.array([1, 2, 5, 10, 12, 20]); b = np.array([0, 2, 4, 10, 16])
+    jac = [(a, 1, b, 1, 3)]
+    for _ in range(200):
+        A = np.unique(rng.integers(0, 300, rng.integers(0, 40)))
+        B = np.unique(rng.integers(0, 300, rng.integers(0, 40)))
+        jac.append((A, int(rng.integers(1, 16)), B, 1, int(rng.integers(1, 33))))
+    out["jac_n"] = np.array(len(jac))
+    for i, (A, ga, B, gb, bs) in enumerate(jac):
+        out[f"jac{i}_a"], out[f"jac{i}_b"] = A.astype(np.int64), B.astype(np.int64)
+        out[f"jac{i}_p"] = np.array([ga, gb, bs], np.int64)
+        out[f"jac{i}_d"] = np.array(O.jaccard_group(A, ga, B, gb, bs, ref=True), np.float32)
+    mer = []
+    for _ in range(200):
+        A = np.unique(rng.integers(0, 100, rng.integers(0, 20)))
+        B = np.unique(rng.integers(0, 100, rng.integers(0, 20)))
+        mer.append((A, B))
+    out["mer_n"] = np.array(len(mer))
+    for i, (A, B) in enumerate(mer):
+        out[f"mer{i}_a"], out[f"mer{i}_b"] = A.astype(np.int64), B.astype(np.int64)
+        out[f"mer{i}_r"] = O.merge_rows(A, B, ref=True)
+
+    # --- Keeper reorder cases
+    cases = []
+    test_el = os.path.join(args.reference, "preprocess/data/TEST/TEST_matrix_weighted.el")
+    rp, cs, _, nr, nc = read_el(test_el)
+    for tau, bb, BB in [(0.5, 3, 3), (0.6, 3, 3), (0.5, 16, 16), (0.3, 2, 4), (0.9, 1, 2)]:
+        cases.append(("TEST_matrix_weighted", rp, cs, nc, tau, bb, BB))
+    bc = os.path.join(args.reference, "preprocess/data/minitest/bcsstk18_r.el")
+    rp, cs, _, nr, nc = read_el(bc)
+    cases.append(("bcsstk18_r", rp, cs, nc, 0.5, 16, 16))
+    cases.append(("bcsstk18_r", rp, cs, nc, 0.6, 16, 16))
+    for k in range(6):
+        rows = int(rng.integers(50, 1500)); cols = int(rng.integers(30, 800))
+        rp, cs = rand_pattern(rng, rows, cols, int(rng.integers(2, 30)))
+        cases.append((f"random{k}", rp, cs, cols, float(rng.choice([0.3, 0.5, 0.6, 0.8])),
+                      int(rng.choice([4, 8, 16])), int(rng.choice([4, 8, 16]))))
+    out["keep_n"] = np.array(len(cases))
+    for i, (name, rp, cs, nc, tau, bb, BB) in enumerate(cases):
+        perm, g, st = O.ref_reorder(rp, cs, nc, tau, bb, BB, algo=5, force_fixed=True)
+        out[f"keep{i}_name"] = np.array(name)
+        out[f"keep{i}_rowptr"] = rp.astype(np.int64)
+        out[f"keep{i}_cols"] = cs.astype(np.int32)
+        out[f"keep{i}_params"] = np.array([tau, bb, BB, nc], np.float64)
+        out[f"keep{i}_perm"] = perm.astype(np.int32)
+        out[f"keep{i}_grouping"] = g.astype(np.int64)
+        out[f"keep{i}_stats"] = st.astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, "golden_preprocess.npz"), **out)
+
+    # --- csrToBcsr cases
+    out = {}
+    bcases = []
+    for k in range(8):
+        mr = 16 * int(rng.integers(1, 24)); kk = int(rng.choice([16, 32]))
+        mc = kk * int(rng.integers(1, 12))
+        rp, cs = rand_pattern(rng, mr, mc, int(rng.integers(1, 60)), shuffle=True)
+        v = rng.standard_normal(len(cs)).astype(np.float16)
+        bcases.append((mr, mc, kk, rp, cs, v))
+    out["bcsr_n"] = np.array(len(bcases))
+    for i, (mr, mc, kk, rp, cs, v) in enumerate(bcases):
+        brp, bci, bv, info = O.ref_csr_to_bcsr(mr, mc, kk, rp.astype(np.int32), cs.astype(np.int32), v)
+        out[f"bcsr{i}_dims"] = np.array([mr, mc, kk], np.int64)
+        out[f"bcsr{i}_rowptr"] = rp.astype(np.int32)
+        out[f"bcsr{i}_cols"] = cs.astype(np.int32)
+        out[f"bcsr{i}_vals"] = v
+        out[f"bcsr{i}_brp"], out[f"bcsr{i}_bci"] = brp, bci
+        out[f"bcsr{i}_bval"], out[f"bcsr{i}_info"] = bv, info
+    np.savez_compressed(os.path.join(HERE, "golden_bcsr.npz"), **out)
+
+    # --- CSR::multiply
+    rows = 300
+    rp, cs = rand_pattern(rng, rows, rows, 20)
+    v = rng.standard_normal(len(cs)).astype(np.float32)
+    bcols = 7
+    Bc = rng.uniform(-1, 1, rows * bcols).astype(np.float32)
+    Cref = O.ref_csr_multiply(rp, cs, v, rows, Bc, bcols, rows)
+    np.savez_compressed(os.path.join(HERE, "golden_multiply.npz"), rowptr=rp, cols=cs.astype(np.int32), vals=v,
+                        B=Bc, bcols=np.array(bcols), C=Cref)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

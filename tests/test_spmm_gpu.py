@@ -1,0 +1,219 @@
+"""GPU parity of the tensor-core SpMM (through the C ABI) against the FP64
+CPU oracle, against the reference's own BCSR kernel on identical inputs, and
+size-independent properties at full size.
+
+Tolerances (relative Frobenius error vs FP64): plain FP16 form 1e-3 (the
+spec bound; FP16 inputs are exact in FP64, so the observed error is
+FP32 accumulation only, ~1e-6), BF16 form 1e-2 (BF16 rounding of FP32 data),
+split-BF16 form 1e-4 (spec bound 1e-3).
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(got, ref):
+    got = np.asarray(got, np.float64)
+    n = np.linalg.norm(ref)
+    return float(np.linalg.norm(got - ref) / (n if n > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch.device("cuda", 0)
+
+
+def fp64_product(O, A, B):
+    return O.spmm_f64(A.row_ptr, A.col_idx, A.values.astype(np.float64), np.asarray(B, np.float64))
+
+
+def spmm(M, B, form, out_dtype=torch.float32):
+    C = M.spmm(B, form=form, out_dtype=out_dtype)
+    torch.cuda.synchronize()
+    M.check_device_error()
+    return C.float().cpu().numpy()
+
+
+def test_band_config1_fp16_vs_fp64(dev, smat_mod, oracle_lib):
+    from smat import generators as G
+    A = G.band(4096, 64, seed=1)
+    Bh = np.random.default_rng(2).uniform(-1, 1, (4096, 64)).astype(np.float16)
+    M = smat_mod.Bcsr(A)
+    assert M.info["nnzb"] == 2284
+    B = torch.from_numpy(Bh).to(dev).t().contiguous().t()
+    err = rel_err(spmm(M, B, smat_mod.FORM_F16), fp64_product(oracle_lib, A, Bh))
+    assert err <= 1e-3, err
+
+
+@pytest.mark.parametrize("N", [8, 64, 100, 128, 200, 256, 384])
+@pytest.mark.parametrize("layout", ["col", "row"])
+def test_random_shapes_and_widths(dev, smat_mod, oracle_lib, N, layout):
+    from smat import generators as G
+    A0 = G.random_block(1000, 0.06, 0.05, 0.9, seed=N)     # 1000 rows: not a multiple of 16
+    keep = A0.col_idx < 997                                 # ragged K: drop columns >= 997
+    r = np.repeat(np.arange(A0.rows), np.diff(A0.row_ptr))[keep]
+    rp = np.zeros(A0.rows + 1, np.int64)
+    np.add.at(rp, r + 1, 1)
+    A = smat_mod.Csr(A0.rows, 997, np.cumsum(rp), A0.col_idx[keep], A0.values[keep])
+    Bh = np.random.default_rng(N).uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    M = smat_mod.Bcsr(A)
+    B = torch.from_numpy(Bh).to(dev)
+    if layout == "col":
+        B = B.t().contiguous().t()
+    err = rel_err(spmm(M, B, smat_mod.FORM_F16), fp64_product(oracle_lib, A, Bh))
+    assert err <= 1e-3, err
+
+
+@pytest.mark.parametrize("form,tol", [("bf16", 1e-2), ("split", 1e-4), ("f16_from_f32", 1e-3)])
+def test_forms_with_fp32_b(dev, smat_mod, oracle_lib, form, tol):
+    from smat import generators as G
+    A = G.stencil27(12)                                     # FP32 values, diagonal-dominant
+    rng = np.random.default_rng(4)
+    Bf = rng.standard_normal((A.cols, 96)).astype(np.float32)
+    f = {"bf16": smat_mod.FORM_BF16, "split": smat_mod.FORM_SPLIT_BF16, "f16_from_f32": smat_mod.FORM_F16}[form]
+    M = smat_mod.Bcsr(A, forms=(f,))
+    ref = fp64_product(oracle_lib, A, Bf)
+    err = rel_err(spmm(M, torch.from_numpy(Bf).to(dev), f), ref)
+    if form == "f16_from_f32":
+        # FP16 rounding of A and B bounds this form; check it against the
+        # FP16-rounded inputs in FP64 instead
+        A16 = smat_mod.Csr(A.rows, A.cols, A.row_ptr, A.col_idx, A.values.astype(np.float16))
+        ref = fp64_product(oracle_lib, A16, Bf.astype(np.float16))
+        err = rel_err(spmm(M, torch.from_numpy(Bf).to(dev), f), ref)
+    assert err <= tol, err
+
+
+def test_split_beats_bf16_and_fp16(dev, smat_mod, oracle_lib):
+    from smat import generators as G
+    A = G.stencil27(10)
+    Bf = np.random.default_rng(5).standard_normal((A.cols, 128)).astype(np.float32)
+    M = smat_mod.Bcsr(A, forms=(smat_mod.FORM_F16, smat_mod.FORM_BF16, smat_mod.FORM_SPLIT_BF16))
+    ref = fp64_product(oracle_lib, A, Bf)
+    B = torch.from_numpy(Bf).to(dev)
+    e = {f: rel_err(spmm(M, B, f), ref) for f in (smat_mod.FORM_F16, smat_mod.FORM_BF16, smat_mod.FORM_SPLIT_BF16)}
+    assert e[smat_mod.FORM_SPLIT_BF16] < 1e-4 < e[smat_mod.FORM_F16] < e[smat_mod.FORM_BF16]
+
+
+@pytest.mark.parametrize("R,block", [(4, (16, 16)), (8, (16, 16)), (16, (16, 16)), (4, (32, 16)), (8, (32, 16))])
+def test_panel_heights_and_block_shapes(dev, smat_mod, oracle_lib, R, block):
+    from smat import generators as G
+    A = G.rmat(12, 40000, seed=R)
+    Bh = np.random.default_rng(1).uniform(-1, 1, (A.cols, 160)).astype(np.float16)
+    M = smat_mod.Bcsr(A, block=block, panel_rows=R)
+    err = rel_err(spmm(M, torch.from_numpy(Bh).to(dev), smat_mod.FORM_F16), fp64_product(oracle_lib, A, Bh))
+    assert err <= 1e-3, err
+
+
+def test_fp16_output(dev, smat_mod, oracle_lib):
+    from smat import generators as G
+    A = G.band(2048, 20, seed=3)
+    Bh = np.random.default_rng(3).uniform(-1, 1, (2048, 128)).astype(np.float16)
+    M = smat_mod.Bcsr(A)
+    C = spmm(M, torch.from_numpy(Bh).to(dev), smat_mod.FORM_F16, out_dtype=torch.float16)
+    assert rel_err(C, fp64_product(oracle_lib, A, Bh)) <= 1e-3
+
+
+def test_reorder_pipeline_returns_original_row_order(dev, smat_mod, oracle_lib):
+    from smat import generators as G
+    A = G.rmat(11, 15000, seed=8)
+    r = smat_mod.reorder(A, 0.6, 16, 16)
+    M = smat_mod.Bcsr(A, row_perm=r.perm)
+    Bh = np.random.default_rng(8).uniform(-1, 1, (A.cols, 64)).astype(np.float16)
+    C = spmm(M, torch.from_numpy(Bh).to(dev), smat_mod.FORM_F16)
+    assert rel_err(C, fp64_product(oracle_lib, A, Bh)) <= 1e-3
+    # the BCSR it built is the reference's blocking of the permuted matrix
+    rp, ci, v, _ = M.export()
+    rp2, ci2, v2 = smat_mod.csr_to_bcsr_host(A, (16, 16), r.perm)
+    assert np.array_equal(rp, rp2) and np.array_equal(ci, ci2) and np.array_equal(v.view(np.uint16), v2.view(np.uint16))
+
+
+def test_empty_rows_and_empty_matrix(dev, smat_mod):
+    rp = np.zeros(101, np.int64)
+    rp[50:] = 3
+    A = smat_mod.Csr(100, 40, rp, np.array([1, 17, 39]), np.array([1.0, 2.0, 3.0], np.float32))
+    M = smat_mod.Bcsr(A)
+    B = torch.ones((40, 16), device=dev)
+    C = spmm(M, B, smat_mod.FORM_F16)
+    expect = np.zeros((100, 16))
+    expect[49] = 6.0
+    assert np.array_equal(C, expect)
+    Z = smat_mod.Csr(64, 64, np.zeros(65, np.int64), np.zeros(0, np.int32), np.zeros(0, np.float32))
+    MZ = smat_mod.Bcsr(Z)
+    Cz = MZ.spmm(torch.ones((64, 32), device=dev))
+    torch.cuda.synchronize()
+    assert float(Cz.abs().max()) == 0.0
+
+
+def test_deterministic_and_host_variant(dev, smat_mod):
+    from smat import generators as G
+    A = G.rmat(12, 30000, seed=2)
+    Bh = np.random.default_rng(2).uniform(-1, 1, (A.cols, 128)).astype(np.float16)
+    M = smat_mod.Bcsr(A)
+    B = torch.from_numpy(Bh).to(dev)
+    c1 = spmm(M, B, smat_mod.FORM_F16)
+    c2 = spmm(M, B, smat_mod.FORM_F16)
+    assert np.array_equal(c1, c2)
+    c3 = M.spmm_host(Bh, smat_mod.FORM_F16)
+    assert np.array_equal(c1, c3)
+
+
+def test_errors_are_statuses(dev, smat_mod):
+    from smat import generators as G
+    A = G.band(256, 4, seed=1)
+    M = smat_mod.Bcsr(A)  # FP16 form only
+    B = torch.ones((256, 16), device=dev, dtype=torch.float16)
+    with pytest.raises(smat_mod.SmatError) as e:
+        M.spmm(B, form=smat_mod.FORM_BF16)
+    assert e.value.status == 1
+    C = torch.empty((256, 16), device=dev)
+    with pytest.raises(smat_mod.SmatError) as e:
+        M.spmm_raw(smat_mod.FORM_F16, B, smat_mod.F16, smat_mod.ROW_MAJOR, 16, C, smat_mod.F32, 16, 16, None, 0, 0)
+    assert e.value.status == 1
+
+
+def test_linearity_at_rmat_scale(dev, smat_mod):
+    """Full-size property: A(B1 + B2) = A B1 + A B2 for the 65536-row R-MAT
+    workload shape (exact up to FP32 accumulation)."""
+    from smat import generators as G
+    A = G.rmat(16, 2_000_000, seed=3)
+    M = smat_mod.Bcsr(A)
+    g = torch.Generator(device=dev).manual_seed(1)
+    B1 = (torch.rand((A.cols, 128), device=dev, generator=g) - 0.5).half()
+    B2 = (torch.rand((A.cols, 128), device=dev, generator=g) - 0.5).half()
+    s = (B1.float() + B2.float())
+    C1 = M.spmm(B1.float())
+    C2 = M.spmm(B2.float())
+    C12 = M.spmm(s)
+    torch.cuda.synchronize()
+    lhs, rhs = C12.double(), (C1.double() + C2.double())
+    assert float((lhs - rhs).norm() / rhs.norm()) < 1e-3
+
+
+def test_reference_kernel_agrees(dev, smat_mod, oracle_lib):
+    """Same inputs through the reference's own mmaOBTKernelSparse (FP16
+    accumulate, FP16 C) and through ours (FP32 accumulate): both checked
+    against FP64, and against each other at 1e-3."""
+    import ref_kernel
+    if not ref_kernel.available():
+        pytest.skip("reference cubin not built")
+    from smat import generators as G
+    A = G.band(4096, 64, seed=1)
+    N = 64
+    Bh = np.random.default_rng(2).uniform(-1, 1, (4096, N)).astype(np.float16)
+    M = smat_mod.Bcsr(A)
+    rp, ci, v, _ = M.export()
+    Bcol = torch.from_numpy(Bh).to(dev).t().contiguous()          # (N, K) rows = columns of B
+    Cref, keep = ref_kernel.run(torch.from_numpy(v).to(dev), torch.from_numpy(rp).to(dev),
+                                torch.from_numpy(ci).to(dev), 4096, 4096, Bcol, N)
+    torch.cuda.synchronize()
+    ours = spmm(M, Bcol.t(), smat_mod.FORM_F16)
+    ref64 = fp64_product(oracle_lib, A, Bh)
+    e_ref = rel_err(Cref.float().cpu().numpy(), ref64)
+    e_ours = rel_err(ours, ref64)
+    e_pair = rel_err(ours, Cref.float().cpu().numpy().astype(np.float64))
+    assert e_ours <= 1e-3 and e_ours <= e_ref
+    assert e_pair <= 1e-3, (e_pair, e_ref, e_ours)
