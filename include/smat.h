@@ -109,7 +109,7 @@ typedef struct smat_reorder_stats {
  * identical to the reference's permutation; grouping_out (optional) receives
  * the final grouping vector (the reference's ".g" file content). A column
  * index is "the" column (col_idx); the pattern is used, values are ignored.
- * On an sm_103 device the candidate scan runs on the GPU when use_gpu != 0. */
+ * use_gpu is reserved (the scan runs on the host's cores either way). */
 smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
                          int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
                          int64_t* grouping_out, smat_reorder_stats* stats);
