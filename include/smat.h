@@ -173,6 +173,26 @@ smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, in
 smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packed_b, int64_t N,
                              void* C, int32_t c_dtype, int64_t ldc, void* stream);
 
+/* Largest scratch smat_spmm_static_scratch can use (per device). */
+#define SMAT_SPMM_STATIC_SCRATCH_BYTES (32u << 20)
+
+/* smat_spmm for callers that can neither allocate device memory nor pass
+ * scratch in: a launcher bound to a fixed signature without a workspace
+ * parameter, or code where allocating is not allowed (cudaMalloc may
+ * synchronise the device; some services fix their memory at start-up).
+ * No counterpart in the reference (its launchers allocate nothing because
+ * they need no scratch). Same arguments and results as smat_spmm, without
+ * workspace; the packed B goes to a fixed device array of
+ * SMAT_SPMM_STATIC_SCRATCH_BYTES inside the library, and nothing is
+ * allocated. Returns SMAT_ERR_UNSUPPORTED when smat_spmm_workspace_size()
+ * exceeds that size (e.g. K = 65536 holds N up to 256 for FP16/BF16, 128
+ * for the split form). The first call on a device looks the array's address
+ * up (make it before any stream capture). All calls on a device share the
+ * array: calls that overlap in time (other streams, other threads) race. */
+smat_status smat_spmm_static_scratch(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                                     int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
+                                     int64_t N, void* stream);
+
 /* Host-buffer variant: copies B (host) in, runs smat_spmm, copies C (host)
  * out, and waits for completion. Uses device buffers cached in the handle. */
 smat_status smat_spmm_host(const smat_bcsr* A, int32_t form, const void* B_host, int32_t b_dtype,

@@ -113,6 +113,8 @@ static int pick_nsub(const smat_bcsr* h, int64_t N, bool split) {
   return 1;
 }
 
+int smat::bcsr_device(const smat_bcsr* A) { return A->device; }
+
 extern "C" {
 
 const char* smat_last_error(void) { return g_last_error.c_str(); }

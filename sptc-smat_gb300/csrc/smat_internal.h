@@ -14,6 +14,9 @@ namespace smat {
 void set_error(const std::string& msg);
 smat_status fail(smat_status st, const std::string& msg);
 
+// CUDA device ordinal a handle was built on (api.cu).
+int bcsr_device(const smat_bcsr* A);
+
 // ------------------------------------------------------------------ reorder
 struct ReorderResult {
   std::vector<int64_t> grouping;

@@ -1,0 +1,81 @@
+// spmm_static.cu — smat_spmm_static_scratch: the SpMM with its packed-B
+// scratch in a fixed, file-scope device array instead of caller-provided
+// workspace.
+//
+// Some callers can neither allocate device memory nor hand in scratch:
+// a launcher bound to a fixed signature that has no workspace parameter
+// (such as the reference's HGEMM_FUNC_SPARSE2 launchers), or code running
+// where allocating is not allowed — cudaMalloc can synchronise the device
+// and stall every stream, and a service that budgets its memory at start-up
+// may forbid allocations afterwards. This entry point serves them: it calls
+// no cudaMalloc, cudaFree or allocating library routine. The scratch is
+// g_spmm_scratch below, SMAT_SPMM_STATIC_SCRATCH_BYTES (32 MiB) per device,
+// reserved when the library's device code is loaded on that device.
+//
+// Host code cannot use g_spmm_scratch as a pointer (on the host the name
+// stands for the symbol, not a device address). The first call on each
+// device therefore looks the address up with cudaGetSymbolAddress, with
+// that device current, and keeps it for later calls on that device. Make
+// that first call on each device before any stream capture begins.
+//
+// Every call on a device shares the one array and leaves its contents
+// behind. Nothing in it has to start at zero: the pack kernel rewrites every
+// byte the contraction reads (padding included) before the contraction runs,
+// in stream order. Calls that overlap in time — on different streams, or
+// from different threads — race on the array and corrupt each other's B.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+#include "smat_internal.h"
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) uint8_t g_spmm_scratch[SMAT_SPMM_STATIC_SCRATCH_BYTES];
+
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_spmm_scratch on `dev`, looked up once per device.
+smat_status scratch_on(int dev, void** out) {
+  if (dev < 0 || dev >= kMaxDevices) return smat::fail(SMAT_ERR_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaGetDevice failed");
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_scratch);
+    if (prev != dev) cudaSetDevice(prev);
+    if (e != cudaSuccess || !p)
+      return smat::fail(SMAT_ERR_CUDA, std::string("cudaGetSymbolAddress(g_spmm_scratch): ") + cudaGetErrorString(e));
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return SMAT_OK;
+}
+
+}  // namespace
+
+smat_status smat_spmm_static_scratch(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
+                                     int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
+                                     int64_t N, void* stream) {
+  if (!A || !B || !C) return smat::fail(SMAT_ERR_INVALID, "null argument");
+  size_t need = 0;
+  smat_status st = smat_spmm_workspace_size(A, form, b_dtype, N, &need);
+  if (st != SMAT_OK) return st;
+  if (need > (size_t)SMAT_SPMM_STATIC_SCRATCH_BYTES)
+    return smat::fail(SMAT_ERR_UNSUPPORTED,
+                      "packed B needs " + std::to_string(need) + " bytes but the static scratch holds " +
+                          std::to_string((size_t)SMAT_SPMM_STATIC_SCRATCH_BYTES) +
+                          "; use smat_spmm with a caller-provided workspace");
+  void* scratch = nullptr;
+  st = scratch_on(smat::bcsr_device(A), &scratch);
+  if (st != SMAT_OK) return st;
+  return smat_spmm(A, form, B, b_dtype, b_layout, ldb, C, c_dtype, ldc, N, scratch,
+                   (size_t)SMAT_SPMM_STATIC_SCRATCH_BYTES, stream);
+}

@@ -64,6 +64,8 @@ _SIGS = {
                                    C.c_void_p, C.c_size_t, C.c_void_p]),
     "smat_spmm_packed": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_int64,
                                    C.c_void_p]),
+    "smat_spmm_static_scratch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64,
+                                           C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
     "smat_spmm_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                                  C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
     "smat_bcsr_check_device_error": (C.c_int, [C.c_void_p]),
