@@ -340,8 +340,9 @@ def run_smat(args):
     stored = 2.0 * nnzb * 256 * N
     value = world * useful / (ms * 1e-3) / 1e12
     nbr = info["rows_padded"] // 16
-    # contraction kernel: A blocks (FP16) + 1 metadata byte per block + panel table + packed B once + C (FP32)
-    alg_bytes = nnzb * 256 * 2 + nnzb + 32 * info["n_panels"] + A.cols * N * 2 + A.rows * N * 4
+    # contraction kernel, BCSR minimum: FP16 block values + one 4-byte column index per block + block-row
+    # pointers, B once (FP16, packed) and C once (FP32)
+    alg_bytes = nnzb * (256 * 2 + 4) + (nbr + 1) * 4 + A.cols * N * 2 + A.rows * N * 4
     peak, peak_kind = peaks()
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
     tr = profile_traffic()

@@ -98,6 +98,35 @@ typedef struct smat_reorder_stats {
   int64_t merges;               /* rows merged under tau (merge_counter) */
 } smat_reorder_stats;
 
+/* ---------------------------------------------------------------- files */
+
+/* A CSR read from a file; the arrays belong to the library (release them
+ * with smat_csr_file_free). */
+typedef struct smat_csr_file {
+  smat_csr csr;       /* values: SMAT_F64 from MatrixMarket, SMAT_F32 from edge lists, NULL for patterns */
+  int32_t symmetric;  /* MatrixMarket symmetric/hermitian file, expanded */
+} smat_csr_file;
+
+/* MatrixMarket coordinate file -> CSR, as mmio_allinone + padSparseMatrix
+ * (src/cuda_hgemm/src/common/mmio_highlevel.h:514-680): rows padded to a
+ * multiple of 16, columns to a multiple of col_pad (the block width), entries
+ * in file order, symmetric/hermitian files mirrored (the mirrored entry right
+ * after its source), complex files keep the real part, pattern values 1.0.
+ * Values are the parsed doubles (FP16 conversion happens once, later). */
+smat_status smat_read_mtx(const char* path, int32_t col_pad, smat_csr_file* out);
+
+/* Edge list "row col [value]" -> CSR, as CSR::read_from_edgelist
+ * (preprocess/src/general/csr.cpp:166-290) with its defaults (space
+ * delimiter, general matrix): rows ascending, cols = max column + 1, FP32
+ * values unless pattern_only. */
+smat_status smat_read_el(const char* path, int32_t pattern_only, smat_csr_file* out);
+
+/* Pattern edge list of A with new row r = old row row_perm[r] (NULL: as is):
+ * the *_reordered.el file Matrix_Blocking writes (csr.cpp:150-161). */
+smat_status smat_write_el(const char* path, const smat_csr* A, const int64_t* row_perm);
+
+smat_status smat_csr_file_free(smat_csr_file* f);
+
 /* ---------------------------------------------------------------- step 1 */
 
 /* Row reordering. Replaces `Matrix_Blocking -f x.el -a algo -b col_block
@@ -165,7 +194,7 @@ smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b
 /* The two halves of smat_spmm, for callers that reuse one B with several
  * matrices or want to time the contraction alone: smat_spmm_pack_b writes B
  * into `workspace` in the tensor-core tile layout (4 KB tiles of 16 rows x
- * 128 columns, 32-byte swizzled; hi and lo halves for the split form);
+ * 128 columns, 32-byte swizzled; 8 KB hi+lo pairs for the split form);
  * smat_spmm_packed runs the contraction from that packed copy. */
 smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
                              int32_t b_layout, int64_t ldb, int64_t N, void* workspace,

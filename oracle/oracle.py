@@ -92,6 +92,11 @@ def ref_pre():
                                   C.c_int, _i64p, _i64p, _i64p]
         L.ref_csr_multiply.restype = None
         L.ref_csr_multiply.argtypes = [C.c_int64, C.c_int64, _i64p, _i64p, _f32p, _f32p, C.c_int64, _f32p]
+        L.ref_read_el.restype = C.c_int64
+        L.ref_read_el.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.POINTER(C.c_int64)),
+                                  C.POINTER(C.POINTER(C.c_int64)), C.POINTER(C.POINTER(C.c_float))]
+        L.ref_pre_free.restype = None
+        L.ref_pre_free.argtypes = [C.c_void_p]
         L.ref_csr_reorder_rows.restype = None
         L.ref_csr_reorder_rows.argtypes = [C.c_int64, C.c_int64, _i64p, _i64p, _f32p, _i64p, _i64p, _i64p, _f32p]
         _ref_pre = L
@@ -258,3 +263,45 @@ def csr_multiply_f32_range(ld, r0, r1, rowptr, colidx, val, B_colmajor, b_cols, 
     """CSR::multiply's loop over rows [r0, r1); arrays must stay alive (raw pointers)."""
     lib().orc_csr_multiply_f32_range(ld, r0, r1, rowptr.ctypes.data, colidx.ctypes.data, val.ctypes.data,
                                      B_colmajor.ctypes.data, b_cols, C_colmajor.ctypes.data)
+
+
+def ref_read_mtx(path, k=16):
+    """The reference's mmio_allinone (mmio_highlevel.h:523-680) on a file:
+    (rows, cols, symmetric, rowptr int32, colidx int32, values as FP16 bits)."""
+    L = ref_bcsr_lib()
+    m, n, z = C.c_int64(), C.c_int64(), C.c_int64()
+    sym = C.c_int()
+    rp, ci, v = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)(), C.POINTER(C.c_uint16)()
+    rc = L.ref_read_mtx(os.fsencode(path), k, C.byref(m), C.byref(n), C.byref(z), C.byref(sym), C.byref(rp),
+                        C.byref(ci), C.byref(v))
+    if rc != 0:
+        raise RuntimeError(f"reference mmio_allinone failed: {rc}")
+    try:
+        rowptr = np.ctypeslib.as_array(rp, (m.value + 1,)).copy()
+        colidx = np.ctypeslib.as_array(ci, (z.value,)).copy() if z.value else np.zeros(0, np.int32)
+        vals = np.ctypeslib.as_array(v, (z.value,)).copy() if z.value else np.zeros(0, np.uint16)
+    finally:
+        for p in (rp, ci, v):
+            L.ref_free(C.cast(p, C.c_void_p))
+    return m.value, n.value, sym.value, rowptr, colidx, vals
+
+
+def ref_read_el(path, pattern_only=False):
+    """The reference's CSR::read_from_edgelist (csr.cpp:166-290) on a file:
+    (rows, cols, rowptr int64, colidx int64, values float32), or None if it threw."""
+    L = ref_pre()
+    cols = C.c_int64()
+    rp, ci, v = C.POINTER(C.c_int64)(), C.POINTER(C.c_int64)(), C.POINTER(C.c_float)()
+    rows = L.ref_read_el(os.fsencode(path), 1 if pattern_only else 0, C.byref(cols), C.byref(rp), C.byref(ci),
+                         C.byref(v))
+    if rows < 0:
+        return None
+    try:
+        rowptr = np.ctypeslib.as_array(rp, (rows + 1,)).copy()
+        nnz = int(rowptr[-1])
+        colidx = np.ctypeslib.as_array(ci, (nnz,)).copy() if nnz else np.zeros(0, np.int64)
+        vals = np.ctypeslib.as_array(v, (nnz,)).copy() if nnz else np.zeros(0, np.float32)
+    finally:
+        for p in (rp, ci, v):
+            L.ref_pre_free(C.cast(p, C.c_void_p))
+    return rows, cols.value, rowptr, colidx, vals

@@ -6,8 +6,11 @@
 // struct (preprocess/include/matrices.h:10-86) in memory and calls the
 // reference functions unchanged. Used only by tests to pin the oracle and to
 // generate golden fixtures.
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <new>
 #include <vector>
 
@@ -111,6 +114,45 @@ void ref_reorder(int64_t rows, int64_t cols, const int64_t* rowptr, const int64_
   }
   free_csr(c);
 }
+
+// CSR::read_from_edgelist (csr.cpp:166-290) with Matrix_Blocking's defaults
+// (space delimiter, edge-list format, no symmetrisation). Returns the row
+// count (or -1 if the reference threw); the outputs are malloc'd arrays the
+// caller releases with ref_pre_free.
+int64_t ref_read_el(const char* path, int pattern_only, int64_t* cols, int64_t** rowptr, int64_t** colidx,
+                    float** val) {
+  void* mem = ::operator new(sizeof(CSR));
+  std::memset(mem, 0, sizeof(CSR));
+  CSR* c = reinterpret_cast<CSR*>(mem);
+  std::ifstream in(path);
+  try {
+    c->read_from_edgelist(in, " ", pattern_only != 0, el, false);
+  } catch (...) {
+    ::operator delete(mem);
+    return -1;
+  }
+  int64_t nnz = 0;
+  for (intT i = 0; i < c->rows; i++) nnz += c->nzcount[i];
+  *cols = c->cols;
+  *rowptr = static_cast<int64_t*>(std::malloc((c->rows + 1) * sizeof(int64_t)));
+  *colidx = static_cast<int64_t*>(std::malloc(std::max<int64_t>(nnz, 1) * sizeof(int64_t)));
+  *val = static_cast<float*>(std::malloc(std::max<int64_t>(nnz, 1) * sizeof(float)));
+  int64_t p = 0;
+  (*rowptr)[0] = 0;
+  for (intT i = 0; i < c->rows; i++) {
+    for (intT k = 0; k < c->nzcount[i]; k++) {
+      (*colidx)[p] = c->ja[i][k];
+      (*val)[p] = pattern_only ? 1.0f : c->ma[i][k];
+      p++;
+    }
+    (*rowptr)[i + 1] = p;
+  }
+  const int64_t rows = c->rows;
+  free_csr(c);
+  return rows;
+}
+
+void ref_pre_free(void* p) { std::free(p); }
 
 // CSR::multiply (csr.cpp:47-63) on a CSR built in memory: B and C column-major
 // with leading dimension `rows`; C is accumulated in place.

@@ -26,7 +26,7 @@ COMMON = ["-O3", "-std=c++17", f"-I{INCLUDE}", f"-I{CSRC}"]
 HOSTFLAGS = ["-fPIC", "-fopenmp", "-ffp-contract=off"]
 
 CU_SOURCES = ["api.cu", "spmm_tc.cu", "convert.cu", "spmm_static.cu"]
-CPP_SOURCES = ["reorder.cpp", "bcsr.cpp"]
+CPP_SOURCES = ["reorder.cpp", "bcsr.cpp", "io.cpp"]
 
 
 def _cmd_cu(src, obj):

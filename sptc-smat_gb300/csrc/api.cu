@@ -77,11 +77,12 @@ struct smat_bcsr {
   int num_sms = 0;
   int32_t* d_row_map = nullptr;
   PanelInfo* d_panels = nullptr;
-  ChunkRec* d_chunks = nullptr;
+  StageRec* d_stages = nullptr;
   Sched sched[3];  // by NSUB (1, 2)
-  // A blocks in stream order, pre-swizzled, one copy per form: F16, BF16, -, SPLIT hi
+  // A stream per form (F16, BF16, -, SPLIT): per stage the pre-swizzled
+  // blocks in consumption order (hi, then lo for the split form) and the
+  // stage header
   uint8_t* d_aval[4] = {nullptr, nullptr, nullptr, nullptr};
-  uint8_t* d_aval_lo = nullptr;
   int* d_err = nullptr;
   // smat_spmm_host staging
   std::mutex mu;
@@ -98,8 +99,8 @@ static void free_handle(smat_bcsr* h) {
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
-  void* ptrs[] = {h->d_row_map, h->d_chunks, h->d_panels,
-                  h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_aval_lo, h->d_err,
+  void* ptrs[] = {h->d_row_map, h->d_stages, h->d_panels,
+                  h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
                   h->d_bstage, h->d_cstage, h->d_ws, h->sched[1].d_cta_ptr, h->sched[1].d_cta_items,
                   h->sched[2].d_cta_ptr, h->sched[2].d_cta_items};
   for (void* p : ptrs)
@@ -214,7 +215,7 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
   const HostBcsr& b = h->host;
   const Plan& pl = h->plan;
   SMAT_TRY(upload(&h->d_row_map, b.row_map.data(), b.row_map.size()));
-  SMAT_TRY(upload(&h->d_chunks, pl.chunks.data(), pl.chunks.size()));
+  SMAT_TRY(upload(&h->d_stages, pl.stages.data(), pl.stages.size()));
   SMAT_TRY(upload(&h->d_panels, pl.panels.data(), pl.panels.size()));
   {
     int zero = 0;
@@ -227,7 +228,7 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
   std::vector<double> cost(pl.n_panels);
   for (int32_t p = 0; p < pl.n_panels; p++) {
     int64_t tiles = 0;
-    for (int32_t c = 0; c < pl.panels[p].nchunks; c++) tiles += pl.chunks[pl.panels[p].chunk_off + c].ntiles;
+    for (int32_t c = 0; c < pl.panels[p].nstages; c++) tiles += pl.stages[pl.panels[p].stage_off + c].ntiles;
     cost[p] = pl.panels[p].nblk + 2.0 * tiles + 0.5 * R * bh;
   }
   for (int nsub = 1; nsub <= 2; nsub++) {
@@ -241,26 +242,39 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
     SMAT_TRY(upload(&h->sched[nsub].d_cta_items, cta_items.data(), cta_items.size()));
   }
 
-  // A values, one device copy per requested form, in stream order and in the
-  // 32-byte-swizzled shared-memory layout: inside each 256-byte group of 8
-  // rows (32 bytes per row), the two 16-byte halves of rows 4..7 are swapped.
+  // A streams, one per requested form: for each stage its blocks in
+  // consumption order in the 32-byte-swizzled shared-memory layout (inside
+  // each 256-byte group of 8 rows of 32 bytes, the two 16-byte halves of
+  // rows 4..7 are swapped), hi then lo blocks for the split form, then the
+  // stage header.
   const int64_t nnzb = b.nnzb();
   const size_t bsz = (size_t)bh * bw, ablk = (size_t)bh * 32;
-  auto stream_layout = [&](const std::vector<uint16_t>& vals, std::vector<uint8_t>& out) {
-    out.assign(std::max<size_t>(nnzb, 1) * ablk, 0);
-#pragma omp parallel for schedule(static)
-    for (int64_t k = 0; k < nnzb; k++) {
+  const int64_t nst = (int64_t)pl.stages.size();
+  auto stream_layout = [&](const std::vector<uint16_t>& hi, const std::vector<uint16_t>* lo,
+                           std::vector<uint8_t>& out) {
+    const size_t nops = lo ? 2 : 1;
+    out.assign(std::max<size_t>((size_t)nnzb * ablk * nops + pl.headers.size(), 16), 0);
+    auto put = [&](const std::vector<uint16_t>& vals, int64_t k, uint8_t* dst) {
       const uint8_t* src = reinterpret_cast<const uint8_t*>(vals.data() + (size_t)pl.stream_blk[k] * bsz);
-      uint8_t* dst = out.data() + (size_t)k * ablk;
       for (int r = 0; r < bh; r++)
         for (int c = 0; c < 2; c++)
           std::memcpy(dst + r * 32 + ((c ^ ((r >> 2) & 1)) * 16), src + r * 32 + c * 16, 16);
+    };
+#pragma omp parallel for schedule(static)
+    for (int64_t si = 0; si < nst; si++) {
+      const StageRec& r = pl.stages[si];
+      uint8_t* base = out.data() + (size_t)r.blk_off * ablk * nops + (size_t)r.hdr_off;
+      for (int32_t q = 0; q < r.nblk; q++) {
+        put(hi, r.blk_off + q, base + (size_t)q * ablk);
+        if (lo) put(*lo, r.blk_off + q, base + ((size_t)r.nblk + q) * ablk);
+      }
+      std::memcpy(base + (size_t)r.nblk * ablk * nops, pl.headers.data() + r.hdr_off, (size_t)r.hdr_bytes);
     }
   };
   std::vector<uint8_t> lay;
   const size_t nval = (size_t)nnzb * bsz;
   if (forms & (1u << SMAT_FORM_F16)) {
-    stream_layout(b.val_f16, lay);
+    stream_layout(b.val_f16, nullptr, lay);
     SMAT_TRY(upload(&h->d_aval[SMAT_FORM_F16], lay.data(), lay.size()));
   }
   if (forms & ((1u << SMAT_FORM_BF16) | (1u << SMAT_FORM_SPLIT_BF16))) {
@@ -269,12 +283,13 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
       hi[i] = f32_to_bf16_bits(b.val[i]);
       lo[i] = f32_to_bf16_bits(b.val[i] - bf16_bits_to_f32(hi[i]));
     }
-    stream_layout(hi, lay);
-    if (forms & (1u << SMAT_FORM_BF16)) SMAT_TRY(upload(&h->d_aval[SMAT_FORM_BF16], lay.data(), lay.size()));
+    if (forms & (1u << SMAT_FORM_BF16)) {
+      stream_layout(hi, nullptr, lay);
+      SMAT_TRY(upload(&h->d_aval[SMAT_FORM_BF16], lay.data(), lay.size()));
+    }
     if (forms & (1u << SMAT_FORM_SPLIT_BF16)) {
+      stream_layout(hi, &lo, lay);
       SMAT_TRY(upload(&h->d_aval[SMAT_FORM_SPLIT_BF16], lay.data(), lay.size()));
-      stream_layout(lo, lay);
-      SMAT_TRY(upload(&h->d_aval_lo, lay.data(), lay.size()));
     }
   }
   // keep the FP16 values for export; the FP32 copy is no longer needed
@@ -375,11 +390,10 @@ smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, in
   DeviceGuard guard(A->device);
   if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
   const bool split = form == SMAT_FORM_SPLIT_BF16;
-  uint8_t* hi = static_cast<uint8_t*>(workspace);
-  uint8_t* lo = split ? hi + need / 2 : nullptr;
+  uint8_t* out = static_cast<uint8_t*>(workspace);
   const int in_dt = b_dtype == SMAT_F32 ? 0 : (b_dtype == SMAT_F16 ? 1 : 2);
   const int mode = form == SMAT_FORM_F16 ? 0 : (split ? 2 : 1);
-  cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, hi, lo, K, N,
+  cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, out, K, N,
                          static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "pack_b");
   return SMAT_OK;
@@ -401,18 +415,14 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   const int bh = hb.bh, R = A->plan.R;
   if (!tc_variant_supported(bh, R, nsub, split)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
   const Sched& sc = A->sched[nsub];
-  size_t need = 0;
-  smat_spmm_workspace_size(A, form, SMAT_F16, N, &need);
   SpmmArgs args;
   std::memset(&args, 0, sizeof(args));
   const uint32_t BN = 128u * nsub;
   args.bpack = static_cast<const uint8_t*>(packed_b);
-  args.bpack2 = split ? args.bpack + need / 2 : nullptr;
   args.bp_ntiles = packed_b_tiles(N);
   args.aval = A->d_aval[form];
-  if (split) args.aval2 = A->d_aval_lo;
   args.panels = A->d_panels;
-  args.chunks = A->d_chunks;
+  args.stages = A->d_stages;
   args.cta_ptr = sc.d_cta_ptr;
   args.cta_items = sc.d_cta_items;
   args.row_map = A->d_row_map;

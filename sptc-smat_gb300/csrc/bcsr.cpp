@@ -166,10 +166,13 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
   plan.n_panels = (int32_t)((nbr + R - 1) / R);
   const int32_t P = plan.n_panels;
   if (b.nnzb() >= ((int64_t)1 << 31) - 1) return fail(SMAT_ERR_UNSUPPORTED, "too many blocks");
+  const int32_t SB = kStageRows / b.bh;                      // blocks per stage
+  const int32_t max_len = std::min<int32_t>(16, kMaxGroupN / b.bh);
   // MMA-issuing warp owning a slot: kMmaWarps equal ranges of slots
   auto owner = [R](uint32_t slot) -> uint32_t { return (uint32_t)((slot * kMmaWarps) / (uint32_t)R); };
   struct Local {
-    std::vector<ChunkRec> chunks;
+    std::vector<StageRec> stages;
+    std::vector<uint8_t> hdr;
     std::vector<int32_t> blk;
     PanelInfo info{};
     int64_t groups = 0, tiles = 0;
@@ -178,6 +181,7 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
 #pragma omp parallel
   {
     std::vector<std::pair<int64_t, int32_t>> ent;  // (col * 32 + slot, block)
+    std::vector<std::pair<uint32_t, uint32_t>> mma;  // (owner, entry) of the stage being built
 #pragma omp for schedule(dynamic, 16)
     for (int32_t p = 0; p < P; p++) {
       Local& L = loc[p];
@@ -192,93 +196,110 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
       std::sort(ent.begin(), ent.end());
       L.info.nblk = (int32_t)ent.size();
       L.info.slot_mask = mask;
-      // accumulate flags in stream order
-      std::vector<uint16_t> acc(ent.size(), 0);
+      // accumulate flags in stream order: the first block of a slot overwrites
+      std::vector<uint8_t> acc(ent.size(), 0);
       uint32_t touched = 0;
       for (size_t t = 0; t < ent.size(); t++) {
         const uint32_t slot = (uint32_t)(ent[t].first % 32);
-        if ((touched >> slot) & 1u) acc[t] = kMetaAcc;
+        if ((touched >> slot) & 1u) acc[t] = 1;
         touched |= 1u << slot;
       }
-      // chunks: whole union columns where they fit
+      // stages: whole block columns where they fit
       size_t t = 0;
       int32_t ucols = 0;
       while (t < ent.size()) {
-        ChunkRec c{};
-        c.nblk = 0;
-        c.ntiles = 0;
-        std::vector<uint16_t> m(kMetaStride, 0);
-        while (t < ent.size()) {
+        StageRec s{};
+        mma.clear();
+        while (t < ent.size() && s.ntiles < kStageTiles && s.nblk < SB) {
           const int64_t col = ent[t].first / 32;
           size_t e = t;
           while (e < ent.size() && ent[e].first / 32 == col) e++;
           const int32_t run = (int32_t)(e - t);
-          const int32_t room = kChunkBlocks - c.nblk;
-          if (room == 0) break;
-          if (run > room && c.nblk > 0 && run <= kChunkBlocks) break;  // keep the column whole
+          const int32_t room = SB - s.nblk;
+          if (run > room && s.nblk > 0 && run <= SB) break;  // keep the column whole
           const int32_t take = std::min(run, room);
-          const int32_t tile = c.ntiles++;
-          c.kb[tile] = (int32_t)(col / 16);
+          const int32_t tile = s.ntiles++;
+          s.kb[tile] = (int32_t)(col / 16);
           if (t == 0 || ent[t - 1].first / 32 != col) ucols++;
           // MMA groups among the taken blocks
           for (int32_t g = 0; g < take;) {
             const uint32_t slot0 = (uint32_t)(ent[t + g].first % 32);
             int32_t len = 1;
-            while (g + len < take && len < 16) {
+            while (g + len < take && len < max_len) {
               const uint32_t sl = (uint32_t)(ent[t + g + len].first % 32);
               if (sl != slot0 + (uint32_t)len) break;
               if (acc[t + g + len] != acc[t + g]) break;
               if (owner(sl) != owner(slot0)) break;
               len++;
             }
-            for (int32_t q = 0; q < len; q++) {
-              const int32_t pos = c.nblk + g + q;
-              const uint32_t sl = (uint32_t)(ent[t + g + q].first % 32);
-              uint16_t w = (uint16_t)(sl | acc[t + g + q] | (owner(sl) << kMetaOwnerShift) |
-                                      ((uint32_t)tile << kMetaTileShift));
-              if (q == 0) w |= (uint16_t)(len << kMetaLenShift);
-              m[pos] = w;
-            }
+            const uint32_t pos = (uint32_t)(s.nblk + g);
+            const uint32_t entry = pos | ((uint32_t)tile << 5) | (slot0 << 9) | ((uint32_t)(len - 1) << 14) |
+                                   (acc[t + g] ? kEntAccBit : 0u);
+            mma.push_back({owner(slot0), entry});
             L.groups++;
             g += len;
           }
           for (int32_t q = 0; q < take; q++) L.blk.push_back(ent[t + q].second);
-          c.nblk += take;
+          s.nblk += take;
           t += take;
         }
-        L.tiles += c.ntiles;
-        for (int q = 0; q < kMetaStride; q++) c.meta[q] = m[q];
-        L.chunks.push_back(c);
+        L.tiles += s.ntiles;
+        // header: per-warp (first, count), nblk, then the entries grouped by warp
+        std::stable_sort(mma.begin(), mma.end(),
+                         [](const std::pair<uint32_t, uint32_t>& x, const std::pair<uint32_t, uint32_t>& y) {
+                           return x.first < y.first;
+                         });
+        const int32_t ne = (int32_t)mma.size();
+        s.hdr_bytes = (kStageHdrFixed + 4 * ne + 15) / 16 * 16;
+        const size_t h0 = L.hdr.size();
+        L.hdr.resize(h0 + s.hdr_bytes, 0);
+        uint8_t* h = L.hdr.data() + h0;
+        uint16_t wl[kMmaWarps] = {0, 0, 0, 0};
+        for (int32_t i = 0; i < ne; i++) {
+          const uint32_t w = mma[i].first;
+          if ((wl[w] >> 8) == 0) wl[w] = (uint16_t)i;
+          wl[w] = (uint16_t)((wl[w] & 0xffu) | (((wl[w] >> 8) + 1u) << 8));
+          std::memcpy(h + kStageHdrFixed + 4 * i, &mma[i].second, 4);
+        }
+        std::memcpy(h, wl, sizeof(wl));
+        const uint16_t nb16 = (uint16_t)s.nblk;
+        std::memcpy(h + 8, &nb16, 2);
+        L.stages.push_back(s);
       }
-      L.info.nchunks = (int32_t)L.chunks.size();
+      L.info.nstages = (int32_t)L.stages.size();
       L.info.nucol = ucols;
     }
   }
   // concatenate
-  int64_t nch = 0, nb = 0;
+  int64_t nst = 0, nb = 0, nh = 0;
   for (auto& L : loc) {
-    nch += (int64_t)L.chunks.size();
+    nst += (int64_t)L.stages.size();
     nb += (int64_t)L.blk.size();
+    nh += (int64_t)L.hdr.size();
   }
-  if (nch >= ((int64_t)1 << 31)) return fail(SMAT_ERR_UNSUPPORTED, "plan too large");
+  if (nst >= ((int64_t)1 << 31)) return fail(SMAT_ERR_UNSUPPORTED, "plan too large");
   plan.panels.resize(P);
-  plan.chunks.resize(nch);
+  plan.stages.resize(nst);
   plan.stream_blk.resize(nb);
+  plan.headers.resize(nh);
   plan.n_groups = 0;
   plan.n_tiles = 0;
-  int64_t co = 0, bo = 0;
+  int64_t so = 0, bo = 0, ho = 0;
   for (int32_t p = 0; p < P; p++) {
     Local& L = loc[p];
-    L.info.chunk_off = (int32_t)co;
+    L.info.stage_off = (int32_t)so;
     plan.panels[p] = L.info;
-    for (size_t c = 0; c < L.chunks.size(); c++) {
-      ChunkRec r = L.chunks[c];
-      r.blk_off = (int32_t)bo;
+    std::copy(L.blk.begin(), L.blk.end(), plan.stream_blk.begin() + bo);
+    std::copy(L.hdr.begin(), L.hdr.end(), plan.headers.begin() + ho);
+    for (size_t c = 0; c < L.stages.size(); c++) {
+      StageRec r = L.stages[c];
+      r.blk_off = bo;
+      r.hdr_off = ho;
       bo += r.nblk;
-      plan.chunks[co + c] = r;
+      ho += r.hdr_bytes;
+      plan.stages[so + c] = r;
     }
-    std::copy(L.blk.begin(), L.blk.end(), plan.stream_blk.begin() + (bo - (int64_t)L.blk.size()));
-    co += (int64_t)L.chunks.size();
+    so += (int64_t)L.stages.size();
     plan.n_groups += L.groups;
     plan.n_tiles += L.tiles;
   }

@@ -10,7 +10,8 @@
 // (inside every 8-row group the two 16-byte halves of rows 4..7 are swapped).
 // Tiles are ordered [kb][t]; K is zero-padded to 16 and N to 128 (to 256
 // when there is more than one tile, so that 256-column tiles stay in range).
-// The split form writes hi = bf16(b) and lo = bf16(b - hi) to two buffers.
+// The split form writes hi = bf16(b) and lo = bf16(b - hi) as one 8 KB
+// [hi tile | lo tile] pair per tile, so a tile is still one copy.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -44,20 +45,52 @@ __device__ __forceinline__ uint4 pack8(const uint16_t* h) {
                     h[6] | ((uint32_t)h[7] << 16));
 }
 
-// One thread per (tile row n, k-block); 128 threads per tile.
+// Element i of a 16-byte vector of T, as float.
+template <typename T>
+__device__ __forceinline__ float vec_elem(const uint4* v, int i);
+template <>
+__device__ __forceinline__ float vec_elem<float>(const uint4* v, int i) {
+  return __uint_as_float(reinterpret_cast<const uint32_t*>(v)[i]);
+}
+template <>
+__device__ __forceinline__ float vec_elem<__half>(const uint4* v, int i) {
+  return __half2float(__ushort_as_half(reinterpret_cast<const uint16_t*>(v)[i]));
+}
+template <>
+__device__ __forceinline__ float vec_elem<__nv_bfloat16>(const uint4* v, int i) {
+  return __bfloat162float(__ushort_as_bfloat16(reinterpret_cast<const uint16_t*>(v)[i]));
+}
+
+// One thread per (tile row n, k-block); 128 threads per tile. In the
+// column-major layout the 16 k-values of a thread are contiguous and are
+// read as 16-byte vectors where they are aligned and inside K.
 template <typename T, int OUT>
-__global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ hi,
-                             uint8_t* __restrict__ lo, int64_t K, int64_t N, int ntiles) {
+__global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ out,
+                             int64_t K, int64_t N, int ntiles) {
   const int64_t kb = blockIdx.y;
   const int t = blockIdx.x;
   const int r = threadIdx.x;
   const int64_t n = (int64_t)t * 128 + r;
+  constexpr int VEC = 16 / sizeof(T);  // elements per 16-byte vector
+  float xv[16];
+  const T* colp = in + kb * 16 + n * ldi;
+  if (layout == 1 && n < N && kb * 16 + 16 <= K && (reinterpret_cast<uintptr_t>(colp) & 15) == 0) {
+    uint4 v[16 / VEC];
+#pragma unroll
+    for (int q = 0; q < 16 / VEC; q++) v[q] = __ldg(reinterpret_cast<const uint4*>(colp) + q);
+#pragma unroll
+    for (int i = 0; i < 16; i++) xv[i] = vec_elem<T>(&v[i / VEC], i % VEC);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int64_t k = kb * 16 + i;
+      xv[i] = (k < K && n < N) ? load_f<T>(layout == 1 ? in + k + n * ldi : in + k * ldi + n) : 0.0f;
+    }
+  }
   uint16_t h[16], l[16];
 #pragma unroll
   for (int i = 0; i < 16; i++) {
-    const int64_t k = kb * 16 + i;
-    float x = 0.0f;
-    if (k < K && n < N) x = load_f<T>(layout == 1 ? in + k + n * ldi : in + k * ldi + n);
+    const float x = xv[i];
     if (OUT == OUT_F16) {
       h[i] = __half_as_ushort(__float2half_rn(x));
     } else {
@@ -68,24 +101,25 @@ __global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, 
   }
   const int64_t tile = kb * ntiles + t;
   const int sw = (r >> 2) & 1;
-  uint4* dst = reinterpret_cast<uint4*>(hi + tile * 4096 + r * 32);
+  constexpr int64_t kTileBytes = OUT == OUT_SPLIT ? 8192 : 4096;
+  uint4* dst = reinterpret_cast<uint4*>(out + tile * kTileBytes + r * 32);
   dst[sw] = pack8(h);
   dst[sw ^ 1] = pack8(h + 8);
   if (OUT == OUT_SPLIT) {
-    uint4* d2 = reinterpret_cast<uint4*>(lo + tile * 4096 + r * 32);
+    uint4* d2 = reinterpret_cast<uint4*>(out + tile * kTileBytes + 4096 + r * 32);
     d2[sw] = pack8(l);
     d2[sw ^ 1] = pack8(l + 8);
   }
 }
 
 template <typename T, int OUT>
-static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* hi, uint8_t* lo, int64_t K, int64_t N,
+static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* out, int64_t K, int64_t N,
                             cudaStream_t s) {
   const int ntiles = (int)packed_b_tiles(N);
   const int64_t kbs = (K + 15) / 16;
   if (kbs == 0 || ntiles == 0) return cudaSuccess;
   dim3 grid((unsigned)ntiles, (unsigned)kbs);
-  pack_b_tiles<T, OUT><<<grid, 128, 0, s>>>((const T*)in, layout, ldi, hi, lo, K, N, ntiles);
+  pack_b_tiles<T, OUT><<<grid, 128, 0, s>>>((const T*)in, layout, ldi, out, K, N, ntiles);
   return cudaGetLastError();
 }
 
@@ -100,14 +134,14 @@ size_t packed_b_bytes(int64_t K, int64_t N) {
   return (size_t)((K + 15) / 16) * (size_t)packed_b_tiles(N) * 4096;
 }
 
-cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* hi,
-                   uint8_t* lo, int64_t K, int64_t N, cudaStream_t s) {
+cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* out,
+                   int64_t K, int64_t N, cudaStream_t s) {
   using namespace dev;
 #define SMAT_PACK(T)                                                                  \
   switch (out_mode) {                                                                 \
-    case OUT_F16: return run_pack<T, OUT_F16>(in, layout, ldi, hi, lo, K, N, s);     \
-    case OUT_BF16: return run_pack<T, OUT_BF16>(in, layout, ldi, hi, lo, K, N, s);   \
-    case OUT_SPLIT: return run_pack<T, OUT_SPLIT>(in, layout, ldi, hi, lo, K, N, s); \
+    case OUT_F16: return run_pack<T, OUT_F16>(in, layout, ldi, out, K, N, s);     \
+    case OUT_BF16: return run_pack<T, OUT_BF16>(in, layout, ldi, out, K, N, s);   \
+    case OUT_SPLIT: return run_pack<T, OUT_SPLIT>(in, layout, ldi, out, K, N, s); \
     default: return cudaErrorInvalidValue;                                            \
   }
   switch (in_dtype) {

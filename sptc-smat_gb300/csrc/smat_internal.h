@@ -54,16 +54,16 @@ smat_status build_host_bcsr(const smat_csr& A, int32_t bh, int32_t bw, const int
                             HostBcsr& out);
 
 // Work plan of the tensor-core SpMM. Panels of `R` block rows; the blocks of
-// a panel are ordered by block column (then block row) and cut into chunks of
-// at most kChunkBlocks blocks; each chunk lists the B tiles (block columns)
-// it needs, and each block carries a metadata word (slot, accumulate flag,
-// MMA group, tile index).
+// a panel are ordered by block column (then block row) and cut into stages
+// of at most kStageRows / bh blocks and kStageTiles block columns. Each stage
+// has a record (StageRec) and a header with its MMA list (spmm_tc.h).
 struct Plan {
   int32_t R = 8;
   int32_t n_panels = 0;
   std::vector<PanelInfo> panels;
-  std::vector<ChunkRec> chunks;
+  std::vector<StageRec> stages;
   std::vector<int32_t> stream_blk;   // BCSR block index at each stream position
+  std::vector<uint8_t> headers;      // stage headers, concatenated (StageRec::hdr_off)
   int64_t n_groups = 0;              // MMA instructions per pass over A
   int64_t n_tiles = 0;               // B tile loads per pass over A
 };

@@ -15,15 +15,17 @@
 // B tile of a column is loaded once and used by every block row of the panel
 // that has a block there. The A blocks are stored on the device in exactly
 // that visiting order, already in the shared-memory layout the MMA reads
-// (32-byte swizzle). The pipeline moves STAGES: one stage carries a chunk of
-// up to kChunkBlocks A blocks, every packed B tile those blocks need and one
-// metadata word per block, so the whole hand-off between the copy engine
-// and the tensor cores is one full/empty barrier pair per chunk.
+// (32-byte swizzle). The pipeline moves STAGES: one stage carries up to 16
+// A blocks (8 of 32 rows), up to 8 packed B tiles those blocks need and the
+// stage's MMA list (precomputed on the host, stored after the stage's A
+// blocks so that one copy brings both), so the hand-off between the copy
+// engine and the tensor cores is one full/empty barrier pair per stage.
 //
 // Roles (512 threads):
-//   warps 8..15     producers: one bulk copy each per stage (a warp keeps
-//                   only about one copy per ~300 cycles in flight): the B
-//                   tiles, the A chunk (warp 15); warp 8 writes the metadata.
+//   warps 8..15     copy warps: a stage needs one bulk copy for its A blocks
+//                   and list and one per B tile; the copies rotate over the
+//                   eight warps (a warp keeps only about one copy at a time
+//                   in flight).
 //   warps 0..3      MMA issuers, lane 0 each, one per quarter of the panel's
 //                   block rows (one thread issues at most one tcgen05.mma
 //                   per ~80-150 cycles; four keep the tensor pipe at its
@@ -68,21 +70,22 @@ template <int BH, int R, int NSUB, int KIND>
 struct Cfg {
   static constexpr int BN = 128 * NSUB;                   // C columns per tile
   static constexpr int NOPS = (KIND == KIND_SPLIT) ? 2 : 1;
-  static constexpr int CH = kChunkBlocks;
-  static constexpr uint32_t ABLK = BH * 32;               // bytes of one A block
-  static constexpr uint32_t TILE = BN * 32;               // bytes of one B tile
-  static constexpr uint32_t OFF_B = CH * ABLK * NOPS;     // stage: A blocks (hi, lo), B tiles (hi, lo), metadata
-  static constexpr uint32_t OFF_META = OFF_B + CH * TILE * NOPS;
-  static constexpr uint32_t STAGE = (OFF_META + kMetaStride * 2 + 1023) / 1024 * 1024;
-  // one CTA per SM for R >= 16 (TMEM) or wide stages, two below
-  static constexpr uint32_t BUDGET = 200 * 1024;
-  static constexpr int NS_FIT = (int)(BUDGET / STAGE);
+  static constexpr int SB = kStageRows / BH;              // A blocks per stage (at most)
+  static constexpr uint32_t ABLK = BH * 32;               // bytes of one A block (one operand)
+  static constexpr uint32_t TILE = BN * 32;               // bytes of one B tile (one operand)
+  static constexpr uint32_t TILEB = TILE * NOPS;          // bytes of one B tile slot
+  // stage: [A blocks hi | lo | header] [B tiles] [header offset word]
+  static constexpr uint32_t OFF_B = (SB * ABLK * NOPS + kStageHdrMax + 1023) / 1024 * 1024;
+  static constexpr uint32_t OFF_HW = OFF_B + kStageTiles * TILEB;
+  static constexpr uint32_t STAGE = (OFF_HW + 16 + 1023) / 1024 * 1024;
+  static constexpr uint32_t SMEM_AVAIL = 227 * 1024 - 2048;  // minus alignment slack and barriers
+  static constexpr int NS_FIT = (int)(SMEM_AVAIL / STAGE);
   static constexpr int NS = NS_FIT < 2 ? 2 : (NS_FIT > 8 ? 8 : NS_FIT);  // stages
   static constexpr uint32_t SUB_COLS = R * BH;            // TMEM columns of one 128-column subtile
   static constexpr uint32_t ACC_COLS = NSUB * SUB_COLS;   // TMEM columns per buffer
   static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
   static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
-  static constexpr int NPROD = 8;                         // producer warps
+  static constexpr int NPROD = 8;                         // copy warps
   static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA);
   static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 16;
   static constexpr int THREADS = 512;
@@ -90,7 +93,10 @@ struct Cfg {
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
   static_assert(R <= 32, "slot field is 5 bits");
-  static_assert(CH <= 8 && kMetaStride * 2 == 16, "tile index is 3 bits; metadata is one 16-byte copy");
+  static_assert(SB <= kStageMaxBlocks, "position field is 5 bits, header sized for 16 entries");
+  static_assert(kStageTiles == NPROD, "one copy warp per tile slot");
+  static_assert(NS_FIT >= 2, "two stages must fit");
+  static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
 };
 
 // Wait used only while draining after an abort: bounded, ignores the flag.
@@ -111,8 +117,15 @@ __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volati
   return mbar_try_wait(bar, parity) || mbar_wait(bar, parity, abort, err, where);
 }
 
+__device__ __forceinline__ int shfl_i(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
+  const int lo = __shfl_sync(0xffffffffu, (int)(uint32_t)(uint64_t)v, src);
+  const int hi = __shfl_sync(0xffffffffu, (int)(uint32_t)((uint64_t)v >> 32), src);
+  return (int64_t)(((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo);
+}
+
 // Warp roles (16 warps): 0..3 MMA issuers (0 also owns TMEM), 4..7
-// epilogue (TMEM lane quadrants 0..3), 8..15 producers.
+// epilogue (TMEM lane quadrants 0..3), 8..15 copy warps.
 template <int BH, int R, int NSUB, int KIND>
 __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
   using C = Cfg<BH, R, NSUB, KIND>;
@@ -133,7 +146,7 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < C::NS; i++) {
-      mbar_init(smem_u32(&full[i]), C::NPROD);
+      mbar_init(smem_u32(&full[i]), 1);  // the A copy warp's arrive (+ every copy's bytes)
       mbar_init(smem_u32(&empty[i]), C::NMMA);
     }
     for (int i = 0; i < 2; i++) {
@@ -160,81 +173,89 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
   const uint32_t smem0 = smem_u32(smem);
 
   if (warp >= 8) {
-    // --------------------------------------------------------------- producers
-    // One warp completes only about one bulk copy at a time (~20 B/cycle), so
-    // the copies of every stage are spread over eight producer warps, and the
-    // duties rotate with the stage number c: producer c % 8 copies the
-    // chunk's A blocks (from HBM, the slowest copy) and writes its metadata,
-    // producer (c + 1 + t) % 8 copies B tile t. Each producer arrives once per
-    // stage with the bytes it issued; the stage completes when all eight have
-    // arrived and every copy landed. Chunk records are read 32 at a time (one
-    // per lane) and each lane pre-selects what its warp needs from its record.
+    // ---------------------------------------------------------------- copies
+    // Stage number c (counted over the CTA's whole run) needs 1 + ntiles
+    // bulk copies: copy 0 = the A blocks and the MMA list, copy j = B tile
+    // j - 1. Copy warp p issues the copies j with (j + c) % 8 == p, so every
+    // warp issues about one copy per stage and the A copy (from HBM, the
+    // slowest) rotates. A warp keeps only about one copy at a time in flight,
+    // so spreading them is what keeps the copy engine busy. The warp that
+    // issues copy 0 posts the stage's total byte count (arrive.expect_tx) on
+    // the stage's full barrier; the others only add their bytes as they land.
+    // Stage records are read 32 at a time, one per lane, and each lane
+    // prepares what its warp needs from its record.
     const int pw = warp - 8;
     const uint64_t pol_a = make_l2_policy_evict_first();  // A streams through L2 once
     const uint64_t pol_b = make_l2_policy_evict_last();   // B tiles are re-read by many CTAs
     uint32_t ci = 0;
     bool ok = true;
+    uint32_t last_mine = 0xffffffffu;  // last stage this warp copied into (for the drain)
     for (int it = it0; it < it1 && ok; ++it) {
       const PanelInfo pi = args.panels[args.cta_items[it]];
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
-        for (int base = 0; base < pi.nchunks && ok; base += 32) {
-          const int cnt = min(32, pi.nchunks - base);
-          // this lane's record belongs to stage number ci + lane
+        const int64_t bcol = (int64_t)nt * NSUB;  // first 128-column packed tile of this pass
+        for (int base = 0; base < pi.nstages && ok; base += 32) {
+          const int cnt = min(32, pi.nstages - base);
+          // lane l prepares stage ci + l
           const uint32_t my_ci = ci + (uint32_t)lane;
-          const int my_tile = (int)((uint32_t)pw - my_ci - 1u) & 7;
-          const bool my_a = (int)(my_ci & 7u) == pw;
-          int4 r0 = make_int4(0, 0, 0, 0), r3 = r0;
-          int mykb = 0;
+          const int j0 = (int)(((uint32_t)pw - my_ci) & 7u);
+          int64_t off1 = 0, off2 = 0;
+          int bytes1 = 0, total = 0, hword = 0, has2 = 0;
           if (lane < cnt) {
-            const int4* rp = reinterpret_cast<const int4*>(args.chunks + pi.chunk_off + base + lane);
-            r0 = rp[0];  // blk_off, nblk, ntiles, -
-            const int4 kbv = rp[1 + (my_tile >> 2)];
-            mykb = (my_tile & 3) == 0 ? kbv.x : (my_tile & 3) == 1 ? kbv.y : (my_tile & 3) == 2 ? kbv.z : kbv.w;
-            if (my_a) r3 = rp[3];  // metadata words
+            const StageRec* rp = args.stages + pi.stage_off + base + lane;
+            const int4 r1 = reinterpret_cast<const int4*>(rp)[1];  // nblk, hdr_bytes, ntiles, -
+            const int ntl = r1.z;
+            if (j0 == 0) {
+              const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
+              hword = r1.x * (int)(C::ABLK * C::NOPS);
+              off1 = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
+              bytes1 = hword + r1.y;
+              total = bytes1 + ntl * (int)C::TILEB;
+              if (ntl == kStageTiles) {
+                has2 = 1;
+                off2 = ((int64_t)rp->kb[kStageTiles - 1] * args.bp_ntiles + bcol) * (4096 * C::NOPS);
+              }
+            } else if (j0 <= ntl) {
+              off1 = ((int64_t)rp->kb[j0 - 1] * args.bp_ntiles + bcol) * (4096 * C::NOPS);
+              bytes1 = (int)C::TILEB;
+            }
           }
           for (int i = 0; i < cnt; ++i, ++ci) {
-            const int blk_off = __shfl_sync(0xffffffffu, r0.x, i);
-            const int nblk = __shfl_sync(0xffffffffu, r0.y, i);
-            const int ntiles = __shfl_sync(0xffffffffu, r0.z, i);
-            const int kb = __shfl_sync(0xffffffffu, mykb, i);
-            int4 mv;
-            mv.x = __shfl_sync(0xffffffffu, r3.x, i);
-            mv.y = __shfl_sync(0xffffffffu, r3.y, i);
-            mv.z = __shfl_sync(0xffffffffu, r3.z, i);
-            mv.w = __shfl_sync(0xffffffffu, r3.w, i);
-            const int tile = (int)((uint32_t)pw - ci - 1u) & 7;
-            const bool do_a = (int)(ci & 7u) == pw;
+            const int b1 = shfl_i(bytes1, i);
+            const int h2 = shfl_i(has2, i);
+            const int64_t o1 = shfl_l(off1, i);
+            const int64_t o2 = shfl_l(off2, i);
+            const int tot = shfl_i(total, i);
+            const int hw = shfl_i(hword, i);
+            const int j = (int)(((uint32_t)pw - ci) & 7u);
             int good = 1;
             if (lane == 0) {
               const uint32_t s = ci % C::NS;
+              // Every copy warp waits for every stage, with or without a copy
+              // in it: a parity wait only tells the last two phases apart, so
+              // a warp that skipped a stage could otherwise run a whole ring
+              // ahead and overwrite a stage still in use.
               if (wait_phase(smem_u32(&empty[s]), ((ci / C::NS) & 1) ^ 1, abort_flag, err, ERR_PROD_A)) {
                 const uint32_t st = smem0 + s * C::STAGE;
                 const uint32_t fb = smem_u32(&full[s]);
-                uint32_t bytes = 0;
-                if (tile < ntiles) bytes += C::TILE * C::NOPS;
-                if (do_a) {
-                  bytes += nblk * C::ABLK * C::NOPS;
-                  *reinterpret_cast<int4*>(smem + s * C::STAGE + C::OFF_META) = mv;
+                if (b1 == 0) {
+                  // no copy for this warp in this stage
+                } else if (j == 0) {
+                  *reinterpret_cast<uint32_t*>(smem + s * C::STAGE + C::OFF_HW) = (uint32_t)hw;
+                  mbar_arrive_expect_tx(fb, (uint32_t)tot);
+                  bulk_load_hint(st, args.aval + o1, (uint32_t)b1, fb, pol_a);
+                  if (h2)
+                    bulk_load_hint(st + C::OFF_B + (kStageTiles - 1) * C::TILEB, args.bpack + o2, C::TILEB, fb,
+                                   pol_b);
+                } else {
+                  bulk_load_hint(st + C::OFF_B + (j - 1) * C::TILEB, args.bpack + o1, C::TILEB, fb, pol_b);
                 }
-                mbar_arrive_expect_tx(fb, bytes);
-                if (do_a) {
-                  const size_t aoff = (size_t)blk_off * C::ABLK;
-                  bulk_load_hint(st, args.aval + aoff, nblk * C::ABLK, fb, pol_a);
-                  if (KIND == KIND_SPLIT)
-                    bulk_load_hint(st + C::CH * C::ABLK, args.aval2 + aoff, nblk * C::ABLK, fb, pol_a);
-                }
-                if (tile < ntiles) {
-                  const size_t boff = ((size_t)kb * args.bp_ntiles + (size_t)nt * NSUB) * 4096;
-                  bulk_load_hint(st + C::OFF_B + tile * C::TILE * C::NOPS, args.bpack + boff, C::TILE, fb, pol_b);
-                  if (KIND == KIND_SPLIT)
-                    bulk_load_hint(st + C::OFF_B + tile * C::TILE * C::NOPS + C::TILE, args.bpack2 + boff, C::TILE,
-                                   fb, pol_b);
-                }
+                if (b1 != 0) last_mine = ci;
               } else {
                 good = 0;
               }
             }
-            good = __shfl_sync(0xffffffffu, good, 0);
+            good = shfl_i(good, 0);
             if (!good) {
               ok = false;
               break;
@@ -243,24 +264,25 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
         }
       }
     }
-    if (!ok && lane == 0) {
-      // wait for this warp's own copies still in flight
-      for (uint32_t k = (ci > (uint32_t)C::NS ? ci - C::NS : 0); k < ci; ++k)
+    if (!ok && lane == 0 && last_mine != 0xffffffffu) {
+      // wait for this warp's own copies still in flight: they can only be in
+      // the last NS stages it copied into
+      const uint32_t lo = last_mine + 1 > (uint32_t)C::NS ? last_mine + 1 - C::NS : 0;
+      for (uint32_t k = lo; k <= last_mine; ++k)
         mbar_wait_drain(smem_u32(&full[k % C::NS]), (k / C::NS) & 1, err);
     }
   } else if (warp < C::NMMA) {
     if (lane == 0) {
       // ----------------------------------------------------------- MMA issuers
-      // Issuer w owns the groups whose owner field is w (a quarter of the
-      // panel's block rows) and releases every stage once. One thread can
-      // issue a tcgen05.mma only every ~80-150 cycles; four keep the tensor
-      // pipe at its per-instruction rate for these narrow MMAs.
-      const uint32_t mine = (uint32_t)warp;
+      // Issuer w runs the MMA groups of its quarter of the panel's block rows,
+      // from the list the copy brought in with the stage, and releases every
+      // stage once. One thread issues a tcgen05.mma only every ~80-150
+      // cycles; four keep the tensor pipe near its rate for these narrow MMAs.
       const uint32_t idesc0 = args.idesc;  // without the N field
       uint32_t ci = 0, k = 0;
       bool ok = true, issued = false;
       for (int it = it0; it < it1 && ok; ++it) {
-        const int nchunks = args.panels[args.cta_items[it]].nchunks;
+        const int nstages = args.panels[args.cta_items[it]].nstages;
         for (int nt = 0; nt < n_tiles && ok; ++nt, ++k) {
           const uint32_t buf = k & 1;
           const uint32_t dbase = tmem + buf * C::ACC_COLS;
@@ -269,7 +291,7 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
             break;
           }
           tc_fence_after();
-          for (int c = 0; c < nchunks; ++c, ++ci) {
+          for (int c = 0; c < nstages; ++c, ++ci) {
             const uint32_t s = ci % C::NS;
             // the stage's copies landed (complete_tx); the MMA reads shared
             // memory through the async proxy, so no tcgen05 fence is needed
@@ -277,27 +299,27 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
               ok = false;
               break;
             }
-            const uint4 mv = *reinterpret_cast<const uint4*>(smem + s * C::STAGE + C::OFF_META);
-            const uint32_t mw[4] = {mv.x, mv.y, mv.z, mv.w};
+            const uint8_t* stp = smem + s * C::STAGE;
+            const uint32_t hw = *reinterpret_cast<const uint32_t*>(stp + C::OFF_HW);
+            const uint32_t wl = *reinterpret_cast<const uint16_t*>(stp + hw + 2 * warp);
+            const uint32_t first = wl & 0xffu, cnt = wl >> 8;
+            const uint32_t* ent = reinterpret_cast<const uint32_t*>(stp + hw + kStageHdrFixed) + first;
             // descriptors of operands inside the stage = stage descriptor + offset / 16
             const uint64_t sdesc = desc_kmajor_sw32(smem0 + s * C::STAGE);
-#pragma unroll
-            for (int i = 0; i < C::CH; ++i) {
-              const uint32_t m = (mw[i >> 1] >> ((i & 1) * 16)) & 0xffffu;
-              const uint32_t len = (m >> kMetaLenShift) & 31u;
-              if (len == 0 || ((m >> kMetaOwnerShift) & 3u) != mine) continue;
-              const uint32_t slot = m & 31u, acc = (m >> 5) & 1u;
-              const uint32_t tile = m >> kMetaTileShift;
+            for (uint32_t e = 0; e < cnt; ++e) {
+              const uint32_t m = ent[e];
+              const uint32_t pos = m & 31u, tile = (m >> 5) & 15u, slot = (m >> 9) & 31u;
+              const uint32_t len = ((m >> 14) & 15u) + 1u, acc = (m >> 18) & 1u;
               const uint32_t idesc = idesc0 | (((len * BH) >> 3) << 17);
-              const uint64_t a_hi = sdesc + ((i * C::ABLK) >> 4);
-              const uint64_t b_hi0 = sdesc + ((C::OFF_B + tile * C::TILE * C::NOPS) >> 4);
+              const uint64_t a_hi = sdesc + ((pos * C::ABLK) >> 4);
+              const uint64_t b_hi0 = sdesc + ((C::OFF_B + tile * C::TILEB) >> 4);
 #pragma unroll
               for (int j = 0; j < NSUB; ++j) {
                 const uint32_t dcol = dbase + j * C::SUB_COLS + slot * BH;
                 const uint64_t b_hi = b_hi0 + ((j * 128 * 32) >> 4);
                 umma_f16(dcol, b_hi, a_hi, idesc, acc);
                 if (KIND == KIND_SPLIT) {
-                  const uint64_t a_lo = a_hi + ((C::CH * C::ABLK) >> 4);
+                  const uint64_t a_lo = a_hi + ((hw >> 1) >> 4);  // lo blocks follow the nblk hi blocks
                   const uint64_t b_lo = b_hi + (C::TILE >> 4);
                   umma_f16(dcol, b_hi, a_lo, idesc, 1);
                   umma_f16(dcol, b_lo, a_hi, idesc, 1);

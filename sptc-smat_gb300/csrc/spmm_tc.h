@@ -1,4 +1,5 @@
-// spmm_tc.h — launch interface of the tensor-core SpMM kernels.
+// spmm_tc.h — launch interface of the tensor-core SpMM kernels and the
+// layout of their device work plan.
 #pragma once
 
 #include <cuda.h>
@@ -8,61 +9,68 @@
 
 namespace smat {
 
-// Blocks per pipeline stage. A stage carries one chunk of A blocks (in the
-// order the kernel consumes them), every packed B tile those blocks need,
-// and one 16-bit metadata word per block.
-constexpr int kChunkBlocks = 8;
-// Metadata words per chunk (one 16-byte record field).
-constexpr int kMetaStride = 8;
+// A pipeline STAGE carries up to kStageRows * 16 / bh A blocks of one panel
+// (in the order the kernel consumes them), up to kStageTiles packed B tiles
+// those blocks need, and the stage's MMA list. The limits keep a stage's A
+// part at 8 KB (FP16) and its B part at 32 KB (128-column tiles).
+constexpr int kStageRows = 256;   // A rows per stage: 16 blocks of 16 rows, 8 of 32
+constexpr int kStageTiles = 8;
+constexpr int kMmaWarps = 4;      // MMA-issuing warps; each owns a quarter of the panel's block rows
+constexpr int kMaxGroupN = 256;   // widest tcgen05.mma N (kind::f16, M = 128)
 
-// Per-panel record of the device plan (8 x int32).
+// Per-panel record (8 x int32).
 struct PanelInfo {
-  int32_t chunk_off;  // first chunk of the panel
-  int32_t nchunks;    // chunks in the panel
-  int32_t nblk;       // blocks in the panel
-  int32_t nucol;      // union columns (distinct block columns) of the panel
-  uint32_t slot_mask; // bit s set: block row s of the panel has at least one block
+  int32_t stage_off;   // first stage of the panel
+  int32_t nstages;     // stages of the panel
+  int32_t nblk;        // blocks in the panel
+  int32_t nucol;       // distinct block columns of the panel
+  uint32_t slot_mask;  // bit s set: block row s of the panel has at least one block
   int32_t pad0, pad1, pad2;
 };
 
-// Per-chunk record (16 x int32 = 64 bytes): where its blocks are, the
-// k-block index (column / 16) of each B tile it needs, and the metadata word
-// of each of its blocks (zero past nblk).
-struct ChunkRec {
-  int32_t blk_off;   // first block (stream order)
-  int32_t nblk;      // blocks in the chunk (1..kChunkBlocks)
-  int32_t ntiles;    // distinct block columns = B tiles (1..kChunkBlocks)
+// Per-stage record (64 bytes), read by the copy warps. In the device A
+// stream of a form (ABLK = bh * 32 bytes per block and operand, NOPS = 2 for
+// the split form, else 1) a stage occupies
+//     [nblk * ABLK blocks (hi)][nblk * ABLK blocks (lo, split form only)][header]
+// starting at byte blk_off * ABLK * NOPS + hdr_off, where hdr_off is the sum
+// of the header bytes of all earlier stages.
+struct StageRec {
+  int64_t blk_off;     // blocks before this stage (stream order)
+  int64_t hdr_off;     // header bytes before this stage
+  int32_t nblk;        // A blocks in the stage
+  int32_t hdr_bytes;   // bytes of this stage's header (multiple of 16)
+  int32_t ntiles;      // B tiles (distinct block columns) of the stage, 1..kStageTiles
   int32_t pad;
-  int32_t kb[8];     // k-block of each tile, in order
-  uint16_t meta[8];  // per block
+  int32_t kb[kStageTiles];  // k-block (column / 16) of each tile
 };
 
-// Per-block metadata (16 bits). Blocks of consecutive block rows ("slots")
-// at the same block column form an MMA group: one tcgen05.mma with
-// N = bh * length covers them all (their accumulators are adjacent in TMEM
-// and their A blocks adjacent in shared memory). The group's first block
-// carries the length; the others (and padding) carry length 0.
-//   bits 0-4   slot of the group's first block row
-//   bit  5     accumulate into the existing partial sums (else overwrite)
-//   bits 6-7   MMA-issuing warp that owns the group (slot * 4 / R)
-//   bits 8-12  group length (1..16) on the group's first block, else 0
-//   bits 13-15 index of the group's B tile inside the stage
-constexpr uint16_t kMetaAcc = 1u << 5;
-constexpr int kMetaOwnerShift = 6, kMetaLenShift = 8, kMetaTileShift = 13;
-constexpr int kMmaWarps = 4;
+// Stage header (little-endian), kStageHdrFixed bytes then one 32-bit entry
+// per MMA group, grouped by issuing warp:
+//   uint16 warp_list[4]   bits 0-7 first entry of warp w, bits 8-15 its entry count
+//   uint16 nblk, pad[3]
+//   uint32 entry[...]
+// A group is a run of consecutive block rows ("slots") with a block at the
+// same block column, the same accumulate flag and the same owner; it is one
+// tcgen05.mma with N = bh * len (its accumulators are adjacent in TMEM and
+// its A blocks adjacent in the stage). Entry bits:
+//   0-4 position of the first A block in the stage, 5-8 B tile in the stage,
+//   9-13 first slot, 14-17 len - 1, 18 accumulate (else overwrite).
+constexpr int kStageHdrFixed = 16;
+constexpr int kStageMaxBlocks = 16;
+constexpr uint32_t kEntAccBit = 1u << 18;
+constexpr int kStageHdrMax = kStageHdrFixed + 4 * kStageMaxBlocks;  // 80 bytes
 
 // Kernel arguments (one __grid_constant__ parameter).
 struct SpmmArgs {
-  const uint8_t* bpack;     // B in 4 KB tiles [k-block][128-column tile] (pack_b)
-  const uint8_t* bpack2;    // low halves of B (split form)
-  int64_t bp_ntiles;        // 128-column tiles per k-block in bpack
-  const uint8_t* aval;      // A blocks in stream order, pre-swizzled (bh * 32 bytes each)
-  const uint8_t* aval2;     // low halves of A (split form)
+  const uint8_t* bpack;      // B in 4 KB tiles [k-block][128-column tile] (pack_b); the split
+                             // form stores [hi tile | lo tile] pairs, 8 KB per tile
+  int64_t bp_ntiles;         // 128-column tiles per k-block in bpack
+  const uint8_t* aval;       // A stream of the form (see StageRec)
   const PanelInfo* panels;
-  const ChunkRec* chunks;
-  const int32_t* cta_ptr;   // [grid + 1]
-  const int32_t* cta_items; // panels, per CTA
-  const int32_t* row_map;   // [rows_padded] BCSR row -> C row, or -1
+  const StageRec* stages;
+  const int32_t* cta_ptr;    // [grid + 1]
+  const int32_t* cta_items;  // panels, per CTA
+  const int32_t* row_map;    // [rows_padded] BCSR row -> C row, or -1
   void* C;
   int64_t ldc;
   int32_t N;

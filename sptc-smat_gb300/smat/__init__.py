@@ -16,14 +16,15 @@ the calls raise ``SmatError``.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
 
 from ._lib import (BF16, COL_MAJOR, E4M3, F16, F32, F64, FORM_BF16, FORM_F16, FORM_FP8, FORM_SPLIT_BF16,
-                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrStruct, ReorderStats, SmatError, check, lib, ptr)
+                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrFile, CsrStruct, ReorderStats, SmatError, check, lib, ptr)
 
-__all__ = ["Csr", "Bcsr", "reorder", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
+__all__ = ["Csr", "Bcsr", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
            "FORM_FP8", "FORM_SPLIT_BF16", "F32", "F16", "BF16", "F64", "E4M3", "ROW_MAJOR", "COL_MAJOR"]
 
 _VAL_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float16): F16, np.dtype(np.float64): F64}
@@ -86,6 +87,44 @@ class Csr:
             np.zeros(0, np.int64)
         vals = None if self.values is None else self.values[idx]
         return Csr(self.rows, self.cols, rp, self.col_idx[idx], vals)
+
+
+def _take_file(f: CsrFile) -> Csr:
+    """Copy a library-owned CSR into numpy arrays and release it."""
+    try:
+        c = f.csr
+        rp = np.ctypeslib.as_array(C.cast(c.row_ptr, C.POINTER(C.c_int64)), (c.rows + 1,)).copy()
+        ci = (np.ctypeslib.as_array(C.cast(c.col_idx, C.POINTER(C.c_int32)), (c.nnz,)).copy() if c.nnz
+              else np.zeros(0, np.int32))
+        vals = None
+        if c.values:
+            ct = {F64: C.c_double, F32: C.c_float}[c.values_dtype]
+            vals = (np.ctypeslib.as_array(C.cast(c.values, C.POINTER(ct)), (c.nnz,)).copy() if c.nnz
+                    else np.zeros(0, {F64: np.float64, F32: np.float32}[c.values_dtype]))
+        return Csr(int(c.rows), int(c.cols), rp, ci, vals)
+    finally:
+        lib().smat_csr_file_free(C.byref(f))
+
+
+def read_mtx(path: str, col_pad: int = 16) -> Csr:
+    """MatrixMarket -> Csr the way the SpMM harness reads it (padded, file order, symmetric expanded)."""
+    f = CsrFile()
+    check(lib().smat_read_mtx(os.fsencode(path), col_pad, C.byref(f)))
+    return _take_file(f)
+
+
+def read_el(path: str, pattern_only: bool = False) -> Csr:
+    """Edge list -> Csr the way the preprocessing tool reads it."""
+    f = CsrFile()
+    check(lib().smat_read_el(os.fsencode(path), 1 if pattern_only else 0, C.byref(f)))
+    return _take_file(f)
+
+
+def write_el(path: str, csr: Csr, row_perm=None) -> None:
+    """Pattern edge list with new row r = old row row_perm[r] (the *_reordered.el file)."""
+    perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
+    s = csr.struct()
+    check(lib().smat_write_el(os.fsencode(path), C.byref(s), None if perm is None else perm.ctypes.data))
 
 
 @dataclass

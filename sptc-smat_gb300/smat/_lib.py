@@ -35,6 +35,10 @@ class BcsrOpts(C.Structure):
                 ("panel_rows", C.c_int32)]
 
 
+class CsrFile(C.Structure):
+    _fields_ = [("csr", CsrStruct), ("symmetric", C.c_int32)]
+
+
 class BcsrInfo(C.Structure):
     _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("rows_padded", C.c_int64),
                 ("cols_padded", C.c_int64), ("nnz", C.c_int64), ("nnzb", C.c_int64),
@@ -49,6 +53,10 @@ class ReorderStats(C.Structure):
 
 # every symbol include/smat.h declares, with its ctypes signature
 _SIGS = {
+    "smat_read_mtx": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(CsrFile)]),
+    "smat_read_el": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(CsrFile)]),
+    "smat_write_el": (C.c_int, [C.c_char_p, C.POINTER(CsrStruct), C.c_void_p]),
+    "smat_csr_file_free": (C.c_int, [C.POINTER(CsrFile)]),
     "smat_reorder": (C.c_int, [C.POINTER(CsrStruct), C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(ReorderStats)]),
     "smat_bcsr_create": (C.c_int, [C.POINTER(CsrStruct), C.POINTER(BcsrOpts), C.POINTER(C.c_void_p)]),

@@ -9,7 +9,11 @@ own code (built from its sources by oracle/Makefile into oracle/_ref/):
 * golden_bcsr.npz — SparseMatrix::csrToBcsr (src/cuda_hgemm/src/common/matrix.h)
   block structure and values on seeded random CSRs with file-order columns;
 * golden_multiply.npz — CSR::multiply (preprocess/src/general/csr.cpp) on a
-  seeded case.
+  seeded case;
+* golden_io.npz — mmio_allinone (src/cuda_hgemm/src/common/mmio_highlevel.h)
+  on seeded MatrixMarket files (general, symmetric, pattern, integer,
+  hermitian complex, FP16 rounding edge values) and CSR::read_from_edgelist
+  on seeded edge lists, with the file texts.
 
 Run it where the reference sources are present:
 
@@ -149,6 +153,81 @@ def main():
     Cref = O.ref_csr_multiply(rp, cs, v, rows, Bc, bcols, rows)
     np.savez_compressed(os.path.join(HERE, "golden_multiply.npz"), rowptr=rp, cols=cs.astype(np.int32), vals=v,
                         B=Bc, bcols=np.array(bcols), C=Cref)
+    # --- file readers: mmio_allinone (MatrixMarket) and CSR::read_from_edgelist (edge lists)
+    import tempfile
+    out = {}
+    tmp = tempfile.mkdtemp()
+    mtx_cases = []
+
+    def mtx_text(field, sym, m, n, entries, comment=True):
+        lines = [f"%%MatrixMarket matrix coordinate {field} {sym}"]
+        if comment:
+            lines.append("% generated by make_golden.py")
+        lines.append(f"{m} {n} {len(entries)}")
+        for e in entries:
+            lines.append(" ".join(str(x) for x in e))
+        return "\n".join(lines) + "\n"
+
+    def rand_entries(m, n, cnt, kind, lower=False):
+        es = []
+        for _ in range(cnt):
+            i, j = int(rng.integers(1, m + 1)), int(rng.integers(1, n + 1))
+            if lower and j > i:
+                i, j = j, i
+            if kind == "real":
+                es.append((i, j, repr(float(rng.standard_normal() * 10.0 ** int(rng.integers(-3, 3))))))
+            elif kind == "integer":
+                es.append((i, j, int(rng.integers(-50, 50))))
+            elif kind == "complex":
+                es.append((i, j, repr(float(rng.standard_normal())), repr(float(rng.standard_normal()))))
+            else:
+                es.append((i, j))
+        return es
+
+    mtx_cases.append((mtx_text("real", "general", 37, 53, rand_entries(37, 53, 300, "real")), 16))
+    mtx_cases.append((mtx_text("real", "symmetric", 50, 50, rand_entries(50, 50, 200, "real", lower=True)), 16))
+    mtx_cases.append((mtx_text("pattern", "general", 70, 41, rand_entries(70, 41, 250, "pattern")), 32))
+    mtx_cases.append((mtx_text("integer", "symmetric", 33, 33, rand_entries(33, 33, 90, "integer", lower=True)), 16))
+    mtx_cases.append((mtx_text("complex", "hermitian", 20, 20, rand_entries(20, 20, 60, "complex", lower=True)), 16))
+    # values that sit on FP16 rounding boundaries (ties, subnormals, overflow)
+    edge_vals = ["1.00048828125", "1.0009765625", "1.00146484375", "6.103515625e-05", "2.98e-08", "65504",
+                 "65520", "-65519.99", "1e-9", "3.0517578125e-05"]
+    mtx_cases.append((mtx_text("real", "general", 16, 16, [(k + 1, k + 1, v) for k, v in enumerate(edge_vals)]), 16))
+    out["mtx_n"] = np.array(len(mtx_cases))
+    for i, (text, k) in enumerate(mtx_cases):
+        path = os.path.join(tmp, f"m{i}.mtx")
+        with open(path, "w") as f:
+            f.write(text)
+        m, n, sym, rp, ci, vb = O.ref_read_mtx(path, k)
+        out[f"mtx{i}_text"] = np.array(text)
+        out[f"mtx{i}_k"] = np.array(k)
+        out[f"mtx{i}_shape"] = np.array([m, n, sym], np.int64)
+        out[f"mtx{i}_rowptr"], out[f"mtx{i}_colidx"], out[f"mtx{i}_valbits"] = rp, ci, vb
+
+    el_cases = []
+    lines = ["# comment", "% another"]
+    r = 0
+    for _ in range(120):
+        r += int(rng.integers(0, 3))
+        lines.append(f"{r} {int(rng.integers(0, 90))} {float(rng.standard_normal()):.6g}")
+    el_cases.append(("\n".join(lines) + "\n", 0))
+    lines = []
+    r = 2
+    for _ in range(80):
+        r += int(rng.integers(0, 2))
+        lines.append(f"{r} {int(rng.integers(0, 200))}")
+    el_cases.append(("\n".join(lines) + "\n", 1))
+    out["el_n"] = np.array(len(el_cases))
+    for i, (text, pat) in enumerate(el_cases):
+        path = os.path.join(tmp, f"e{i}.el")
+        with open(path, "w") as f:
+            f.write(text)
+        rows, cols, rp, ci, v = O.ref_read_el(path, pattern_only=bool(pat))
+        out[f"el{i}_text"] = np.array(text)
+        out[f"el{i}_pattern"] = np.array(pat)
+        out[f"el{i}_shape"] = np.array([rows, cols], np.int64)
+        out[f"el{i}_rowptr"], out[f"el{i}_colidx"], out[f"el{i}_vals"] = rp, ci, v
+    np.savez_compressed(os.path.join(HERE, "golden_io.npz"), **out)
     print("golden fixtures written to", HERE)
 
 
