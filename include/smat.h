@@ -76,6 +76,9 @@ typedef struct smat_bcsr_opts {
                              are written back in the ORIGINAL row order */
   int32_t device;         /* CUDA device ordinal */
   int32_t panel_rows;     /* block rows per tensor-core work item (0 = autotuned) */
+  float split_frac;       /* a panel costing more than split_frac x the average per-CTA
+                             work is split into parts over several CTAs (0 = default 1.0,
+                             < 0 = never split) */
 } smat_bcsr_opts;
 
 typedef struct smat_bcsr smat_bcsr; /* opaque handle, immutable after create */
@@ -151,6 +154,16 @@ smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_
  * columns to a multiple of bw (mmio_highlevel.h:514-520). The block structure
  * and values are bit-identical to csrToBcsr on the (optionally permuted) CSR. */
 smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat_bcsr** out);
+/* The same handle from an existing BCSR on the host: the arrays the
+ * reference's SparseMatrix keeps (getBcsrRowPtrHost / getBcsrColIdxHost /
+ * getBcsrValuesHost, matrix.h:475-477): row_ptr[rows/16 + 1], col_idx[nnzb]
+ * (column starts, ascending in each block row), values_f16[nnzb*16*bw] (FP16
+ * bits, row-major per block). Blocks are 16 x 16 or 16 x 32 (block_cols 32,
+ * the reference's "large" blocks, split into two 16 x 16 blocks); rows and
+ * cols are multiples of the block shape. opts.row_perm must be NULL. */
+smat_status smat_bcsr_create_from_bcsr(int64_t rows, int64_t cols, int32_t block_rows, int32_t block_cols,
+                                       int64_t nnzb, const int32_t* row_ptr, const int32_t* col_idx,
+                                       const uint16_t* values_f16, const smat_bcsr_opts* opts, smat_bcsr** out);
 smat_status smat_bcsr_destroy(smat_bcsr* A);
 smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info);
 
@@ -172,8 +185,10 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
 
 /* ---------------------------------------------------------------- step 3 */
 
-/* Bytes of device scratch smat_spmm needs for this form / B dtype / N (the
- * packed copy of B; twice that for the split form). */
+/* Bytes of device scratch smat_spmm needs for this form / B dtype / N: the
+ * packed copy of B (twice that for the split form), and for panels split
+ * over several CTAs for load balance, one counter per split panel and a
+ * partial-sum slab per part. */
 smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
                                      size_t* bytes);
 
@@ -214,8 +229,9 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
  * workspace; the packed B goes to a fixed device array of
  * SMAT_SPMM_STATIC_SCRATCH_BYTES inside the library, and nothing is
  * allocated. Returns SMAT_ERR_UNSUPPORTED when smat_spmm_workspace_size()
- * exceeds that size (e.g. K = 65536 holds N up to 256 for FP16/BF16, 128
- * for the split form). The first call on a device looks the array's address
+ * exceeds that size (the packed B, K x N x 2 bytes or twice that for the
+ * split form, plus the partial sums of panels split for load balance). The
+ * first call on a device looks the array's address
  * up (make it before any stream capture). All calls on a device share the
  * array: calls that overlap in time (other streams, other threads) race. */
 smat_status smat_spmm_static_scratch(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,

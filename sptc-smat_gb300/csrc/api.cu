@@ -65,6 +65,9 @@ struct Sched {
   int grid = 0;
   int32_t* d_cta_ptr = nullptr;
   int32_t* d_cta_items = nullptr;
+  WorkItem* d_items = nullptr;
+  int32_t n_split = 0;  // panels split into parts
+  int32_t n_slabs = 0;  // parts of split panels
 };
 
 struct smat_bcsr {
@@ -102,7 +105,7 @@ static void free_handle(smat_bcsr* h) {
   void* ptrs[] = {h->d_row_map, h->d_stages, h->d_panels,
                   h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
                   h->d_bstage, h->d_cstage, h->d_ws, h->sched[1].d_cta_ptr, h->sched[1].d_cta_items,
-                  h->sched[2].d_cta_ptr, h->sched[2].d_cta_items};
+                  h->sched[1].d_items, h->sched[2].d_cta_ptr, h->sched[2].d_cta_items, h->sched[2].d_items};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (prev >= 0) cudaSetDevice(prev);
@@ -116,81 +119,15 @@ static int pick_nsub(const smat_bcsr* h, int64_t N, bool split) {
 
 int smat::bcsr_device(const smat_bcsr* A) { return A->device; }
 
-extern "C" {
-
-const char* smat_last_error(void) { return g_last_error.c_str(); }
-const char* smat_version(void) { return "smat-gb300 0.1 (sm_103a, tcgen05)"; }
-
-smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
-                         int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
-                         int64_t* grouping_out, smat_reorder_stats* stats) {
-  (void)use_gpu;
-  if (!A || !perm_out) return fail(SMAT_ERR_INVALID, "null argument");
-  if (A->rows < 0 || !A->row_ptr || (A->nnz > 0 && !A->col_idx))
-    return fail(SMAT_ERR_INVALID, "malformed CSR");
-  if (col_block < 1 || row_block < 1) return fail(SMAT_ERR_INVALID, "block sizes must be >= 1");
-  if (A->row_ptr[0] != 0 || A->row_ptr[A->rows] != A->nnz)
-    return fail(SMAT_ERR_INVALID, "row_ptr[0] must be 0 and row_ptr[rows] == nnz");
-  for (int64_t r = 0; r < A->rows; r++)
-    if (A->row_ptr[r + 1] < A->row_ptr[r]) return fail(SMAT_ERR_INVALID, "row_ptr not monotone");
-  for (int64_t k = 0; k < A->nnz; k++)
-    if (A->col_idx[k] < 0) return fail(SMAT_ERR_INVALID, "negative column index");
-  std::vector<int64_t> g;
-  int64_t comparisons = 0, merges = 0;
-  if (algo == 5) {
-    keeper_grouping_host(A->rows, A->row_ptr, A->col_idx, tau, col_block, row_block, g,
-                         comparisons, merges);
-  } else if (algo == 2) {
-    // FixedBlocking (blocking.cpp:551-559)
-    g.resize(A->rows);
-    for (int64_t i = 0; i < A->rows; i++) g[i] = i / row_block;
-  } else {
-    return fail(SMAT_ERR_UNSUPPORTED, "only algorithms 5 (Keeper) and 2 (fixed) are implemented");
-  }
-  if (force_fixed && algo != 2) g = fixed_size_grouping(g, row_block);
-  std::vector<int64_t> p = permutation_of(g);
-  std::copy(p.begin(), p.end(), perm_out);
-  if (grouping_out) std::copy(g.begin(), g.end(), grouping_out);
-  if (stats) {
-    stats->comparisons = comparisons;
-    stats->merges = merges;
-  }
-  return SMAT_OK;
-}
-
-smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat_bcsr** out) {
-  if (!A || !out) return fail(SMAT_ERR_INVALID, "null argument");
-  *out = nullptr;
-  smat_bcsr_opts o{};
-  if (opts) o = *opts;
-  const int bh = o.block_rows ? o.block_rows : 16;
-  const int bw = o.block_cols ? o.block_cols : 16;
-  if (bw != 16 || (bh != 16 && bh != 32))
-    return fail(SMAT_ERR_UNSUPPORTED, "tensor-core path supports 16x16 and 32x16 blocks");
-  uint32_t forms = o.forms ? o.forms : (1u << SMAT_FORM_F16);
-  if (forms & (1u << SMAT_FORM_FP8)) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-    return fail(SMAT_ERR_NO_DEVICE, "no CUDA device");
-  if (o.device < 0 || o.device >= ndev) return fail(SMAT_ERR_INVALID, "bad device ordinal");
-  DeviceGuard guard(o.device);
-  if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
-  cudaDeviceProp prop;
-  SMAT_CUDA(cudaGetDeviceProperties(&prop, o.device));
-  if (prop.major != 10 || prop.minor != 3)
-    return fail(SMAT_ERR_NO_DEVICE, "libsmat kernels are built for sm_103a (GB300) only");
-
-  smat_bcsr* h = new smat_bcsr();
-  h->device = o.device;
-  h->forms = forms;
-  h->use24 = o.use_24;
-  h->num_sms = prop.multiProcessorCount;
-  smat_status st = build_host_bcsr(*A, bh, bw, o.row_perm, h->host);
-  if (st != SMAT_OK) {
-    delete h;
-    return st;
-  }
-  int R = o.panel_rows ? o.panel_rows : (bh == 16 ? 8 : 4);
+// Second half of handle creation, shared by the CSR and BCSR entry points:
+// the work plan, the device copies and the schedules. Frees h on failure.
+static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcsr** out) {
+  const int bh = h->host.bh, bw = h->host.bw;
+  const uint32_t forms = h->forms;
+  smat_status st;
+  // 16 block rows per panel (8 of 32 rows) fill TMEM's 512 columns with two
+  // accumulator buffers; heavy panels are split over CTAs below
+  int R = o.panel_rows ? o.panel_rows : (bh == 16 ? 16 : 8);
   if (!tc_variant_supported(bh, R, 1, false)) {
     delete h;
     return fail(SMAT_ERR_UNSUPPORTED, "unsupported panel_rows for this block height");
@@ -222,24 +159,22 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
     SMAT_TRY(upload(&h->d_err, &zero, 1));
   }
 
-  // per-panel cost in units of one block: its blocks, its B tile loads (a
-  // 4 KB tile moves 8x the bytes of a block, mostly from L2) and a fixed
-  // per-item cost for the epilogue (R*bh rows of C)
-  std::vector<double> cost(pl.n_panels);
-  for (int32_t p = 0; p < pl.n_panels; p++) {
-    int64_t tiles = 0;
-    for (int32_t c = 0; c < pl.panels[p].nstages; c++) tiles += pl.stages[pl.panels[p].stage_off + c].ntiles;
-    cost[p] = pl.panels[p].nblk + 2.0 * tiles + 0.5 * R * bh;
-  }
+  // work items per launch shape (NSUB 1 and 2): heavy panels split into
+  // parts so that no CTA gets much more than the average
   for (int nsub = 1; nsub <= 2; nsub++) {
     if (!tc_variant_supported(bh, R, nsub, false)) continue;
-    int per_sm = tc_ctas_per_sm(bh, R, nsub, false);
-    int workers = std::max(1, std::min(pl.n_panels, h->num_sms * per_sm));
+    const int per_sm = tc_ctas_per_sm(bh, R, nsub, false);
+    const int workers = std::max(1, h->num_sms * per_sm);
+    std::vector<WorkItem> items;
     std::vector<int32_t> cta_ptr, cta_items;
-    assign_items(cost, workers, cta_ptr, cta_items);
-    h->sched[nsub].grid = workers;
-    SMAT_TRY(upload(&h->sched[nsub].d_cta_ptr, cta_ptr.data(), cta_ptr.size()));
-    SMAT_TRY(upload(&h->sched[nsub].d_cta_items, cta_items.data(), cta_items.size()));
+    Sched& sc = h->sched[nsub];
+    const double frac = o.split_frac == 0.0f ? 1.0 : (o.split_frac < 0.0f ? 1e30 : (double)o.split_frac);
+    build_work_items(pl, bh, workers, frac, items, cta_ptr, cta_items, sc.n_split, sc.n_slabs);
+    sc.grid = std::max(1, std::min<int>(workers, (int)items.size()));
+    cta_ptr.resize(sc.grid + 1);  // queues past the item count are empty
+    SMAT_TRY(upload(&sc.d_items, items.data(), items.size()));
+    SMAT_TRY(upload(&sc.d_cta_ptr, cta_ptr.data(), cta_ptr.size()));
+    SMAT_TRY(upload(&sc.d_cta_items, cta_items.data(), cta_items.size()));
   }
 
   // A streams, one per requested form: for each stage its blocks in
@@ -299,6 +234,114 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
   return SMAT_OK;
 }
 
+extern "C" {
+
+const char* smat_last_error(void) { return g_last_error.c_str(); }
+const char* smat_version(void) { return "smat-gb300 0.1 (sm_103a, tcgen05)"; }
+
+smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
+                         int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
+                         int64_t* grouping_out, smat_reorder_stats* stats) {
+  (void)use_gpu;
+  if (!A || !perm_out) return fail(SMAT_ERR_INVALID, "null argument");
+  if (A->rows < 0 || !A->row_ptr || (A->nnz > 0 && !A->col_idx))
+    return fail(SMAT_ERR_INVALID, "malformed CSR");
+  if (col_block < 1 || row_block < 1) return fail(SMAT_ERR_INVALID, "block sizes must be >= 1");
+  if (A->row_ptr[0] != 0 || A->row_ptr[A->rows] != A->nnz)
+    return fail(SMAT_ERR_INVALID, "row_ptr[0] must be 0 and row_ptr[rows] == nnz");
+  for (int64_t r = 0; r < A->rows; r++)
+    if (A->row_ptr[r + 1] < A->row_ptr[r]) return fail(SMAT_ERR_INVALID, "row_ptr not monotone");
+  for (int64_t k = 0; k < A->nnz; k++)
+    if (A->col_idx[k] < 0) return fail(SMAT_ERR_INVALID, "negative column index");
+  std::vector<int64_t> g;
+  int64_t comparisons = 0, merges = 0;
+  if (algo == 5) {
+    keeper_grouping_host(A->rows, A->row_ptr, A->col_idx, tau, col_block, row_block, g,
+                         comparisons, merges);
+  } else if (algo == 2) {
+    // FixedBlocking (blocking.cpp:551-559)
+    g.resize(A->rows);
+    for (int64_t i = 0; i < A->rows; i++) g[i] = i / row_block;
+  } else {
+    return fail(SMAT_ERR_UNSUPPORTED, "only algorithms 5 (Keeper) and 2 (fixed) are implemented");
+  }
+  if (force_fixed && algo != 2) g = fixed_size_grouping(g, row_block);
+  std::vector<int64_t> p = permutation_of(g);
+  std::copy(p.begin(), p.end(), perm_out);
+  if (grouping_out) std::copy(g.begin(), g.end(), grouping_out);
+  if (stats) {
+    stats->comparisons = comparisons;
+    stats->merges = merges;
+  }
+  return SMAT_OK;
+}
+
+// Checks the device and allocates the handle shell.
+static smat_status new_handle(const smat_bcsr_opts& o, uint32_t forms, smat_bcsr** hp) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(SMAT_ERR_NO_DEVICE, "no CUDA device");
+  if (o.device < 0 || o.device >= ndev) return fail(SMAT_ERR_INVALID, "bad device ordinal");
+  DeviceGuard guard(o.device);
+  if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+  cudaDeviceProp prop;
+  SMAT_CUDA(cudaGetDeviceProperties(&prop, o.device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(SMAT_ERR_NO_DEVICE, "libsmat kernels are built for sm_103a (GB300) only");
+  smat_bcsr* h = new smat_bcsr();
+  h->device = o.device;
+  h->forms = forms;
+  h->use24 = o.use_24;
+  h->num_sms = prop.multiProcessorCount;
+  *hp = h;
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat_bcsr** out) {
+  if (!A || !out) return fail(SMAT_ERR_INVALID, "null argument");
+  *out = nullptr;
+  smat_bcsr_opts o{};
+  if (opts) o = *opts;
+  const int bh = o.block_rows ? o.block_rows : 16;
+  const int bw = o.block_cols ? o.block_cols : 16;
+  if (bw != 16 || (bh != 16 && bh != 32))
+    return fail(SMAT_ERR_UNSUPPORTED, "tensor-core path supports 16x16 and 32x16 blocks");
+  const uint32_t forms = o.forms ? o.forms : (1u << SMAT_FORM_F16);
+  if (forms & (1u << SMAT_FORM_FP8)) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
+  smat_bcsr* h = nullptr;
+  smat_status st = new_handle(o, forms, &h);
+  if (st != SMAT_OK) return st;
+  DeviceGuard guard(o.device);
+  st = build_host_bcsr(*A, bh, bw, o.row_perm, h->host);
+  if (st != SMAT_OK) {
+    delete h;
+    return st;
+  }
+  return finish_handle(h, o, out);
+}
+
+smat_status smat_bcsr_create_from_bcsr(int64_t rows, int64_t cols, int32_t block_rows, int32_t block_cols,
+                                       int64_t nnzb, const int32_t* row_ptr, const int32_t* col_idx,
+                                       const uint16_t* values_f16, const smat_bcsr_opts* opts, smat_bcsr** out) {
+  if (!out) return fail(SMAT_ERR_INVALID, "null argument");
+  *out = nullptr;
+  smat_bcsr_opts o{};
+  if (opts) o = *opts;
+  if (o.row_perm) return fail(SMAT_ERR_UNSUPPORTED, "row_perm applies to CSR input only");
+  const uint32_t forms = o.forms ? o.forms : (1u << SMAT_FORM_F16);
+  if (forms & (1u << SMAT_FORM_FP8)) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
+  smat_bcsr* h = nullptr;
+  smat_status st = new_handle(o, forms, &h);
+  if (st != SMAT_OK) return st;
+  DeviceGuard guard(o.device);
+  st = build_host_bcsr_from_blocks(rows, cols, block_rows, block_cols, nnzb, row_ptr, col_idx, values_f16, h->host);
+  if (st != SMAT_OK) {
+    delete h;
+    return st;
+  }
+  return finish_handle(h, o, out);
+}
+
 smat_status smat_bcsr_destroy(smat_bcsr* A) {
   free_handle(A);
   return SMAT_OK;
@@ -353,12 +396,31 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
   return SMAT_OK;
 }
 
+// Workspace layout of one SpMM: [packed B (x2 for the split form)]
+// [per split panel, column tile and TMEM lane quadrant: an int counter]
+// [per part of a split panel and column tile: an R*bh x BN FP32 slab].
+struct WsLayout {
+  size_t counters = 0, counter_bytes = 0, slabs = 0, total = 0;
+};
+static WsLayout ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
+  WsLayout w;
+  const bool split = form == SMAT_FORM_SPLIT_BF16;
+  const size_t one = (packed_b_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
+  w.counters = split ? 2 * one : one;
+  const int nsub = pick_nsub(A, N, split);
+  const Sched& sc = A->sched[nsub];
+  const int64_t bn = 128 * nsub, n_tiles = (std::max<int64_t>(N, 1) + bn - 1) / bn;
+  w.counter_bytes = ((size_t)sc.n_split * n_tiles * 4 * sizeof(int32_t) + 255) / 256 * 256;
+  w.slabs = w.counters + w.counter_bytes;
+  w.total = w.slabs + (size_t)sc.n_slabs * n_tiles * A->plan.R * A->host.bh * bn * sizeof(float);
+  return w;
+}
+
 smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
                                      size_t* bytes) {
   if (!A || !bytes) return fail(SMAT_ERR_INVALID, "null argument");
   (void)b_dtype;
-  const size_t one = (packed_b_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
-  *bytes = (form == SMAT_FORM_SPLIT_BF16) ? 2 * one : one;
+  *bytes = ws_layout(A, form, N).total;
   return SMAT_OK;
 }
 
@@ -425,6 +487,16 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   args.stages = A->d_stages;
   args.cta_ptr = sc.d_cta_ptr;
   args.cta_items = sc.d_cta_items;
+  args.items = sc.d_items;
+  const WsLayout wl = ws_layout(A, form, N);
+  uint8_t* ws = const_cast<uint8_t*>(static_cast<const uint8_t*>(packed_b));
+  args.counters = reinterpret_cast<int32_t*>(ws + wl.counters);
+  args.slabs = reinterpret_cast<float*>(ws + wl.slabs);
+  if (sc.n_split > 0) {
+    // the split panels' counters start at zero in every launch
+    cudaError_t e = cudaMemsetAsync(args.counters, 0, wl.counter_bytes, static_cast<cudaStream_t>(stream_));
+    if (e != cudaSuccess) return cuda_fail(e, "clearing the split-panel counters");
+  }
   args.row_map = A->d_row_map;
   args.C = C;
   args.ldc = ldc;

@@ -159,6 +159,71 @@ smat_status build_host_bcsr(const smat_csr& A, int32_t bh, int32_t bw, const int
   return SMAT_OK;
 }
 
+smat_status build_host_bcsr_from_blocks(int64_t rows, int64_t cols, int32_t bh, int32_t bw, int64_t nnzb,
+                                        const int32_t* row_ptr, const int32_t* col_idx, const uint16_t* vals,
+                                        HostBcsr& out) {
+  if (bh != 16 || (bw != 16 && bw != 32))
+    return fail(SMAT_ERR_UNSUPPORTED, "BCSR input must have 16x16 or 16x32 blocks");
+  if (rows < 0 || cols < 0 || rows % bh || cols % bw)
+    return fail(SMAT_ERR_INVALID, "rows and cols must be multiples of the block shape");
+  if (nnzb < 0 || !row_ptr || (nnzb > 0 && (!col_idx || !vals))) return fail(SMAT_ERR_INVALID, "BCSR arrays missing");
+  const int64_t nbr = rows / bh;
+  if (row_ptr[0] != 0 || row_ptr[nbr] != nnzb) return fail(SMAT_ERR_INVALID, "row_ptr[0] must be 0 and row_ptr[last] == nnzb");
+  for (int64_t r = 0; r < nbr; r++) {
+    if (row_ptr[r + 1] < row_ptr[r]) return fail(SMAT_ERR_INVALID, "row_ptr not monotone");
+    for (int32_t k = row_ptr[r]; k < row_ptr[r + 1]; k++) {
+      if (col_idx[k] < 0 || col_idx[k] >= cols || col_idx[k] % bw)
+        return fail(SMAT_ERR_INVALID, "column start out of range or not a multiple of the block width");
+      if (k > row_ptr[r] && col_idx[k] <= col_idx[k - 1])
+        return fail(SMAT_ERR_INVALID, "block columns must ascend within a block row");
+    }
+  }
+  if (nnzb * (bw / 16) >= ((int64_t)1 << 31) - 1) return fail(SMAT_ERR_UNSUPPORTED, "too many blocks");
+  // 16-column blocks: a 16 x 32 block becomes two, both kept (a zero half
+  // still multiplies B, as in the reference kernels)
+  const int split = bw / 16;
+  const size_t bsz = 256;
+  out.rows = out.rows_p = rows;
+  out.cols = out.cols_p = cols;
+  out.bh = 16;
+  out.bw = 16;
+  out.rowptr.assign(nbr + 1, 0);
+  for (int64_t r = 0; r < nbr; r++) out.rowptr[r + 1] = row_ptr[r + 1] * split;
+  out.colidx.resize(nnzb * split);
+  out.val.resize(nnzb * split * bsz);
+  out.val_f16.resize(nnzb * split * bsz);
+  out.is24.assign(nnzb * split, 0);
+  int64_t nnz = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nnz)
+  for (int64_t k = 0; k < nnzb; k++) {
+    for (int h = 0; h < split; h++) {
+      const int64_t b = k * split + h;
+      out.colidx[b] = col_idx[k] + 16 * h;
+      bool ok = true;
+      for (int rr = 0; rr < 16; rr++) {
+        int grp = 0;
+        for (int c = 0; c < 16; c++) {
+          const uint16_t v = vals[(size_t)k * 16 * bw + rr * bw + 16 * h + c];
+          out.val_f16[b * bsz + rr * 16 + c] = v;
+          out.val[b * bsz + rr * 16 + c] = f16_bits_to_f32(v);
+          const bool nz = (v & 0x7fff) != 0;
+          nnz += nz;
+          grp += nz;
+          if ((c & 3) == 3) {
+            ok = ok && grp <= 2;
+            grp = 0;
+          }
+        }
+      }
+      out.is24[b] = ok ? 1 : 0;
+    }
+  }
+  out.nnz = nnz;
+  out.row_map.resize(rows);
+  for (int64_t r = 0; r < rows; r++) out.row_map[r] = (int32_t)r;
+  return SMAT_OK;
+}
+
 smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
   if (R < 1 || R > 32) return fail(SMAT_ERR_INVALID, "panel rows must be in [1, 32]");
   const int64_t nbr = b.nbr();
@@ -304,6 +369,63 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
     plan.n_tiles += L.tiles;
   }
   return SMAT_OK;
+}
+
+void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
+                      std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
+                      std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs) {
+  // cost of a stage in units of one A block: the block copies, the B tiles
+  // (a 4 KB tile moves 8x the bytes of a block, from L2) and a fixed
+  // per-stage hand-off cost; per item, the epilogue (R * bh rows of C)
+  const int32_t P = pl.n_panels;
+  auto stage_cost = [&](const StageRec& r) { return r.nblk + 2.0 * r.ntiles + 4.0; };
+  std::vector<double> pcost(P, 0.0);
+  double total = 0.0;
+  for (int32_t p = 0; p < P; p++) {
+    for (int32_t c = 0; c < pl.panels[p].nstages; c++) pcost[p] += stage_cost(pl.stages[pl.panels[p].stage_off + c]);
+    pcost[p] += 0.5 * pl.R * bh;
+    total += pcost[p];
+  }
+  const double max_item = std::max(1.0, max_item_frac * total / std::max(1, workers));
+  items.clear();
+  n_split = 0;
+  n_slabs = 0;
+  std::vector<double> icost;
+  for (int32_t p = 0; p < P; p++) {
+    const PanelInfo& pi = pl.panels[p];
+    int32_t parts = (int32_t)std::ceil(pcost[p] / max_item);
+    parts = std::max(1, std::min(parts, pi.nstages));
+    if (parts == 1) {
+      items.push_back(WorkItem{p, 0, pi.nstages, -1, 0, 1, 0, 0});
+      icost.push_back(pcost[p]);
+      continue;
+    }
+    // cut the stages into `parts` ranges of about equal cost
+    const double per = (pcost[p] - 0.5 * pl.R * bh) / parts;
+    int32_t s0 = 0;
+    double acc = 0.0;
+    int32_t part = 0;
+    for (int32_t c = 0; c < pi.nstages; c++) {
+      acc += stage_cost(pl.stages[pi.stage_off + c]);
+      const bool cut = acc >= per * (part + 1) && part < parts - 1 && c + 1 < pi.nstages;
+      if (cut || c + 1 == pi.nstages) {
+        items.push_back(WorkItem{p, s0, c + 1, n_split, part, 0, n_slabs, 0});
+        part++;
+        s0 = c + 1;
+      }
+    }
+    const int32_t made = part;
+    for (int32_t i = (int32_t)items.size() - made; i < (int32_t)items.size(); i++) {
+      items[i].nparts = made;
+      double c = 0.0;
+      for (int32_t st = items[i].s0; st < items[i].s1; st++) c += stage_cost(pl.stages[pi.stage_off + st]);
+      // a part writes its slab; the last one also reads all parts back
+      icost.push_back(c + 0.5 * pl.R * bh * 2);
+    }
+    n_split++;
+    n_slabs += made;
+  }
+  assign_items(icost, workers, cta_ptr, cta_items);
 }
 
 void assign_items(const std::vector<double>& cost, int32_t workers, std::vector<int32_t>& cta_ptr,

@@ -53,6 +53,13 @@ struct HostBcsr {
 smat_status build_host_bcsr(const smat_csr& A, int32_t bh, int32_t bw, const int64_t* row_perm,
                             HostBcsr& out);
 
+// HostBcsr from an existing BCSR (16 x 16 or 16 x 32 blocks, values FP16
+// row-major per block, column starts), e.g. the arrays of the reference's
+// SparseMatrix; 16 x 32 blocks are split into two 16 x 16 blocks.
+smat_status build_host_bcsr_from_blocks(int64_t rows, int64_t cols, int32_t bh, int32_t bw, int64_t nnzb,
+                                        const int32_t* row_ptr, const int32_t* col_idx, const uint16_t* vals,
+                                        HostBcsr& out);
+
 // Work plan of the tensor-core SpMM. Panels of `R` block rows; the blocks of
 // a panel are ordered by block column (then block row) and cut into stages
 // of at most kStageRows / bh blocks and kStageTiles block columns. Each stage
@@ -69,6 +76,15 @@ struct Plan {
 };
 
 smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);
+
+// Work items of one launch shape: panels whose cost exceeds max_item_frac
+// of the per-worker average are split into parts (stage ranges) of about
+// that size; the items are then assigned to `workers` queues. n_split =
+// split panels, n_slabs = their parts (one partial-sum slab per part and
+// column tile).
+void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
+                      std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
+                      std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs);
 
 // Longest-processing-time assignment of items to `workers` queues.
 void assign_items(const std::vector<double>& item_cost, int32_t workers,

@@ -19,10 +19,12 @@
 // that first call on each device before any stream capture begins.
 //
 // Every call on a device shares the one array and leaves its contents
-// behind. Nothing in it has to start at zero: the pack kernel rewrites every
-// byte the contraction reads (padding included) before the contraction runs,
-// in stream order. Calls that overlap in time — on different streams, or
-// from different threads — race on the array and corrupt each other's B.
+// behind. The packed B is rewritten in full (padding included) by the pack
+// kernel before the contraction reads it; the only part that must start at
+// zero, the split-panel counters, is cleared by smat_spmm_packed on the
+// call's stream before each contraction. Calls that overlap in time — on
+// different streams, or from different threads — race on the array and
+// corrupt each other's results.
 #include <cuda_runtime.h>
 
 #include <cstdint>

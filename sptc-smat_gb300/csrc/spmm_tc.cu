@@ -55,6 +55,9 @@ namespace dev {
 
 enum : int { KIND_PLAIN = 0, KIND_SPLIT = 1 };
 
+// Stages between the L2 prefetch of a stage's A region and its copy.
+constexpr int kPrefetchAhead = 8;
+
 // Error sites recorded in the global error word.
 enum : int {
   ERR_PROD_A = 102,
@@ -191,25 +194,29 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
     bool ok = true;
     uint32_t last_mine = 0xffffffffu;  // last stage this warp copied into (for the drain)
     for (int it = it0; it < it1 && ok; ++it) {
-      const PanelInfo pi = args.panels[args.cta_items[it]];
+      const WorkItem wi = args.items[args.cta_items[it]];
+      const int stage0 = args.panels[wi.panel].stage_off;
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
         const int64_t bcol = (int64_t)nt * NSUB;  // first 128-column packed tile of this pass
-        for (int base = 0; base < pi.nstages && ok; base += 32) {
-          const int cnt = min(32, pi.nstages - base);
+        for (int base = wi.s0; base < wi.s1 && ok; base += 32) {
+          const int cnt = min(32, wi.s1 - base);
           // lane l prepares stage ci + l
           const uint32_t my_ci = ci + (uint32_t)lane;
           const int j0 = (int)(((uint32_t)pw - my_ci) & 7u);
-          int64_t off1 = 0, off2 = 0;
-          int bytes1 = 0, total = 0, hword = 0, has2 = 0;
+          int64_t off1 = 0, off2 = 0, pf_off = 0;
+          int bytes1 = 0, total = 0, hword = 0, has2 = 0, pf_bytes = 0;
           if (lane < cnt) {
-            const StageRec* rp = args.stages + pi.stage_off + base + lane;
-            const int4 r1 = reinterpret_cast<const int4*>(rp)[1];  // nblk, hdr_bytes, ntiles, -
+            const StageRec* rp = args.stages + stage0 + base + lane;
+            const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
+            const int4 r1 = reinterpret_cast<const int4*>(rp)[1];           // nblk, hdr_bytes, ntiles, -
             const int ntl = r1.z;
+            // this stage's A region, for the L2 prefetch
+            pf_off = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
+            pf_bytes = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
             if (j0 == 0) {
-              const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
               hword = r1.x * (int)(C::ABLK * C::NOPS);
-              off1 = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
-              bytes1 = hword + r1.y;
+              off1 = pf_off;
+              bytes1 = pf_bytes;
               total = bytes1 + ntl * (int)C::TILEB;
               if (ntl == kStageTiles) {
                 has2 = 1;
@@ -220,7 +227,20 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
               bytes1 = (int)C::TILEB;
             }
           }
+          // A comes from HBM: prefetch each stage's A region into L2 kPrefetchAhead
+          // stages before its copy (the batch's first stages right away, one per
+          // warp), so that the copy the MMA waits for is an L2 hit
+          if (pw < cnt && pw < kPrefetchAhead) {
+            const int64_t po = shfl_l(pf_off, pw);
+            const int pb = shfl_i(pf_bytes, pw);
+            if (lane == 0) bulk_prefetch_l2(args.aval + po, (uint32_t)pb);
+          }
           for (int i = 0; i < cnt; ++i, ++ci) {
+            if (i + kPrefetchAhead < cnt) {
+              const int64_t po = shfl_l(pf_off, i + kPrefetchAhead);
+              const int pb = shfl_i(pf_bytes, i + kPrefetchAhead);
+              if (lane == 0 && (int)(((uint32_t)pw - ci) & 7u) == 0) bulk_prefetch_l2(args.aval + po, (uint32_t)pb);
+            }
             const int b1 = shfl_i(bytes1, i);
             const int h2 = shfl_i(has2, i);
             const int64_t o1 = shfl_l(off1, i);
@@ -282,11 +302,14 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
       uint32_t ci = 0, k = 0;
       bool ok = true, issued = false;
       for (int it = it0; it < it1 && ok; ++it) {
-        const int nstages = args.panels[args.cta_items[it]].nstages;
+        const WorkItem wi = args.items[args.cta_items[it]];
+        const int nstages = wi.s1 - wi.s0;
         for (int nt = 0; nt < n_tiles && ok; ++nt, ++k) {
           const uint32_t buf = k & 1;
           const uint32_t dbase = tmem + buf * C::ACC_COLS;
-          if (!wait_phase(smem_u32(&accempty[buf]), ((k >> 1) & 1) ^ 1, abort_flag, err, ERR_MMA_ACC)) {
+          // use u = k / 2 of this buffer waits for phase u of accempty: the
+          // epilogue's initial zeroing (u = 0), then each drain-and-zero
+          if (!wait_phase(smem_u32(&accempty[buf]), (k >> 1) & 1, abort_flag, err, ERR_MMA_ACC)) {
             ok = false;
             break;
           }
@@ -341,11 +364,27 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
     }
   } else if (warp >= 4) {
     // -------------------------------------------------------------- epilogue
-    const uint32_t q = warp & 3;  // TMEM lane quadrant this warp may access
+    // Warp 4 + q drains TMEM lane quadrant q (C columns q*32 .. q*32+31 of
+    // each 128-column subtile) for every slot, and writes zeros back: the
+    // accumulators are all zero whenever the MMA warps receive a buffer, so
+    // a part that starts in the middle of a panel accumulates onto zero.
+    const uint32_t q = warp & 3;
+    const uint32_t lane_base = tmem + ((q * 32u) << 16);
+    for (uint32_t c = 0; c < 2 * C::ACC_COLS; c += 16) tmem_st_x16_zero(lane_base + c);
+    tmem_st_wait();
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(smem_u32(&accempty[0]));
+      mbar_arrive(smem_u32(&accempty[1]));
+    }
+    constexpr int SLAB = R * BH * C::BN;  // floats per slab
     uint32_t k = 0;
     bool ok = true;
     for (int it = it0; it < it1 && ok; ++it) {
-      const int panel = args.cta_items[it];
+      const WorkItem wi = args.items[args.cta_items[it]];
+      const int panel = wi.panel;
+      const bool split = wi.split >= 0;
       const uint32_t slot_mask = args.panels[panel].slot_mask;
       for (int nt = 0; nt < n_tiles; ++nt, ++k) {
         const uint32_t buf = k & 1;
@@ -354,23 +393,88 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
           break;
         }
         tc_fence_after();
-        const uint32_t dbase = tmem + ((q * 32u) << 16) + buf * C::ACC_COLS;
+        const uint32_t dbase = lane_base + buf * C::ACC_COLS;
+        // slab of (part, column tile): (first slab of the panel + part) * n_tiles + nt
+        float* slab = split ? args.slabs + ((size_t)(wi.slab + wi.part) * n_tiles + nt) * SLAB : nullptr;
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
           if (rb >= args.nbr) break;
           const bool empty_slot = ((slot_mask >> s) & 1u) == 0;
-          const int myrow = lane < BH ? args.row_map[(int64_t)rb * BH + lane] : -1;
+          const int myrow = (!split && lane < BH) ? args.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
-            const int n = nt * C::BN + j * 128 + (int)q * 32 + lane;
+            const int nl = j * 128 + (int)q * 32 + lane;  // column inside the tile
+            const int n = nt * C::BN + nl;
 #pragma unroll
             for (int h = 0; h < BH; h += 16) {
               float v[16];
               if (!empty_slot) {
-                tmem_ld_x16(dbase + j * C::SUB_COLS + s * BH + h, v);
+                const uint32_t ta = dbase + j * C::SUB_COLS + s * BH + h;
+                tmem_ld_x16(ta, v);
+                tmem_st_x16_zero(ta);
               } else {
 #pragma unroll
                 for (int m = 0; m < 16; ++m) v[m] = 0.0f;
+              }
+              if (split) {
+#pragma unroll
+                for (int m = 0; m < 16; ++m) __stcg(slab + (size_t)(s * BH + h + m) * C::BN + nl, v[m]);
+              } else {
+#pragma unroll
+                for (int m = 0; m < 16; ++m) {
+                  const int row = __shfl_sync(0xffffffffu, myrow, h + m);
+                  if (row >= 0 && n < args.N) {
+                    const int64_t off = (int64_t)row * args.ldc + n;
+                    if (args.c_f16)
+                      __stcs(reinterpret_cast<__half*>(args.C) + off, __float2half_rn(v[m]));
+                    else
+                      __stcs(reinterpret_cast<float*>(args.C) + off, v[m]);
+                  }
+                }
+              }
+            }
+          }
+        }
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&accempty[buf]));
+        if (!split) continue;
+        // this warp's part of the slab is written: count it; the warp that
+        // brings the count of its quadrant to nparts adds up all parts
+        __threadfence();
+        __syncwarp();
+        int last = 0;
+        if (lane == 0) {
+          int* ctr = args.counters + ((size_t)wi.split * n_tiles + nt) * 4 + q;
+          last = atomicAdd(ctr, 1) == wi.nparts - 1;
+        }
+        last = __shfl_sync(0xffffffffu, last, 0);
+        if (!last) continue;
+        __threadfence();
+        const float* slab0 = args.slabs + ((size_t)wi.slab * n_tiles + nt) * SLAB;
+        for (int s = 0; s < R; ++s) {
+          const int rb = panel * R + s;
+          if (rb >= args.nbr) break;
+          const int myrow = lane < BH ? args.row_map[(int64_t)rb * BH + lane] : -1;
+#pragma unroll
+          for (int j = 0; j < NSUB; ++j) {
+            const int nl = j * 128 + (int)q * 32 + lane;
+            const int n = nt * C::BN + nl;
+            for (int h = 0; h < BH; h += 16) {
+              // 16 rows at a time: the loads of a part are independent, so
+              // they overlap instead of paying one L2 round trip per row
+              float acc[16];
+#pragma unroll
+              for (int m = 0; m < 16; ++m) acc[m] = 0.0f;
+              const float* src = slab0 + (size_t)(s * BH + h) * C::BN + nl;
+              for (int p = 0; p < wi.nparts; ++p) {
+                float t[16];
+#pragma unroll
+                for (int m = 0; m < 16; ++m) t[m] = __ldcg(src + (size_t)m * C::BN);
+#pragma unroll
+                for (int m = 0; m < 16; ++m) acc[m] += t[m];
+                src += (size_t)n_tiles * SLAB;
               }
 #pragma unroll
               for (int m = 0; m < 16; ++m) {
@@ -378,17 +482,14 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
                 if (row >= 0 && n < args.N) {
                   const int64_t off = (int64_t)row * args.ldc + n;
                   if (args.c_f16)
-                    __stcs(reinterpret_cast<__half*>(args.C) + off, __float2half_rn(v[m]));
+                    __stcs(reinterpret_cast<__half*>(args.C) + off, __float2half_rn(acc[m]));
                   else
-                    __stcs(reinterpret_cast<float*>(args.C) + off, v[m]);
+                    __stcs(reinterpret_cast<float*>(args.C) + off, acc[m]);
                 }
               }
             }
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&accempty[buf]));
       }
     }
   }

@@ -60,6 +60,21 @@ constexpr int kStageMaxBlocks = 16;
 constexpr uint32_t kEntAccBit = 1u << 18;
 constexpr int kStageHdrMax = kStageHdrFixed + 4 * kStageMaxBlocks;  // 80 bytes
 
+// A unit of work of one CTA: stages [s0, s1) of a panel. A panel whose
+// stages are split over several items ("parts", for load balance) has a
+// split index: its parts write partial sums to workspace slabs, and the part
+// that finishes last (an atomic counter per split panel and column tile)
+// adds the slabs and writes C.
+struct WorkItem {
+  int32_t panel;
+  int32_t s0, s1;      // stage range, relative to the panel's first stage
+  int32_t split;       // -1: the whole panel; else index of the split panel
+  int32_t part;        // part number within the split panel
+  int32_t nparts;      // parts of the split panel
+  int32_t slab;        // first slab of the split panel (one per part and column tile)
+  int32_t pad;
+};
+
 // Kernel arguments (one __grid_constant__ parameter).
 struct SpmmArgs {
   const uint8_t* bpack;      // B in 4 KB tiles [k-block][128-column tile] (pack_b); the split
@@ -69,7 +84,10 @@ struct SpmmArgs {
   const PanelInfo* panels;
   const StageRec* stages;
   const int32_t* cta_ptr;    // [grid + 1]
-  const int32_t* cta_items;  // panels, per CTA
+  const int32_t* cta_items;  // work items, per CTA
+  const WorkItem* items;
+  float* slabs;              // partial sums of split panels: [slab][R * bh rows][BN] FP32
+  int32_t* counters;         // [split panels][column tiles], zero before the launch
   const int32_t* row_map;    // [rows_padded] BCSR row -> C row, or -1
   void* C;
   int64_t ldc;

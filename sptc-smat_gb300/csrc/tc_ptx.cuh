@@ -92,6 +92,12 @@ __device__ __forceinline__ void bulk_load_hint(uint32_t dst, const void* src, ui
       "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar), "l"(policy)
       : "memory");
 }
+// Bulk prefetch of global memory into L2 (no shared memory, no completion).
+// Address 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(src)), "r"(bytes)
+               : "memory");
+}
 __device__ __forceinline__ uint64_t make_l2_policy_evict_first() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
@@ -158,6 +164,17 @@ __device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
+
+// Each thread of the warp writes zeros to 16 consecutive 32-bit TMEM
+// columns of its lane, and waits until the stores are done.
+__device__ __forceinline__ void tmem_st_x16_zero(uint32_t taddr) {
+  const uint32_t z = 0;
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+      "r"(z)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Shared-memory matrix descriptor of a K-major operand stored with the
 // 32-byte swizzle: rows of 32 bytes (16 x 16-bit elements = one MMA K step),

@@ -181,7 +181,7 @@ class Bcsr:
     """A BCSR matrix resident on one GPU (the reference's ``SparseMatrix``)."""
 
     def __init__(self, csr: Csr, block=(16, 16), forms=(FORM_F16,), row_perm=None, panel_rows: int = 0,
-                 device: int = 0, use_24: bool = False):
+                 device: int = 0, use_24: bool = False, split_frac: float = 0.0):
         o = BcsrOpts()
         o.block_rows, o.block_cols = block
         o.forms = 0
@@ -192,6 +192,7 @@ class Bcsr:
         o.row_perm = None if self._perm is None else self._perm.ctypes.data
         o.device = device
         o.panel_rows = panel_rows
+        o.split_frac = split_frac
         h = C.c_void_p()
         s = csr.struct()
         check(lib().smat_bcsr_create(C.byref(s), C.byref(o), C.byref(h)))

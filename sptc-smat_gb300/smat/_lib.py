@@ -32,7 +32,7 @@ class CsrStruct(C.Structure):
 class BcsrOpts(C.Structure):
     _fields_ = [("block_rows", C.c_int32), ("block_cols", C.c_int32), ("forms", C.c_uint32),
                 ("use_24", C.c_int32), ("row_perm", C.c_void_p), ("device", C.c_int32),
-                ("panel_rows", C.c_int32)]
+                ("panel_rows", C.c_int32), ("split_frac", C.c_float)]
 
 
 class CsrFile(C.Structure):
@@ -60,6 +60,8 @@ _SIGS = {
     "smat_reorder": (C.c_int, [C.POINTER(CsrStruct), C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(ReorderStats)]),
     "smat_bcsr_create": (C.c_int, [C.POINTER(CsrStruct), C.POINTER(BcsrOpts), C.POINTER(C.c_void_p)]),
+    "smat_bcsr_create_from_bcsr": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.POINTER(BcsrOpts), C.POINTER(C.c_void_p)]),
     "smat_bcsr_destroy": (C.c_int, [C.c_void_p]),
     "smat_bcsr_get_info": (C.c_int, [C.c_void_p, C.POINTER(BcsrInfo)]),
     "smat_bcsr_export": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -77,6 +79,8 @@ _SIGS = {
     "smat_spmm_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                                  C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
     "smat_bcsr_check_device_error": (C.c_int, [C.c_void_p]),
+    "smat_ref_shims_last_status": (C.c_int, []),
+    "smat_ref_shims_release": (C.c_int, []),
     "smat_last_error": (C.c_char_p, []),
     "smat_version": (C.c_char_p, []),
 }
@@ -117,3 +121,32 @@ def ptr(a) -> int:
     if isinstance(a, np.ndarray):
         return a.ctypes.data
     return a.data_ptr()
+
+
+# The reference's kernel launchers (C++ linkage, include/smat_ref_shims.h), by
+# their Itanium-mangled names, with ctypes signatures.
+_HP, _IP, _SZ = C.c_void_p, C.c_void_p, C.c_size_t
+REF_SHIMS = {
+    "mmaOBTKernel": ("_Z12mmaOBTKernelP6__halfPiS1_S0_S0_mmmmS1_S1_",
+                     [_HP, _IP, _IP, _HP, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+    "mmaOBTKernel_large": ("_Z18mmaOBTKernel_largeP6__halfPiS1_S0_S0_mmmmS1_S1_",
+                           [_HP, _IP, _IP, _HP, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+    "mmaOBTSKernel": ("_Z13mmaOBTSKernelP6__halfPiS1_PcS0_S0_S0_mmmmS1_S1_",
+                      [_HP, _IP, _IP, C.c_void_p, _HP, _HP, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+    "mmaOBTSKernel_large": ("_Z19mmaOBTSKernel_largeP6__halfPiS1_PcS0_S0_S0_mmmmS1_S1_",
+                            [_HP, _IP, _IP, C.c_void_p, _HP, _HP, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+    "mmaOBTSKernel_large_separate": ("_Z28mmaOBTSKernel_large_separateP6__halfPiS1_S0_S1_S1_PcS0_S0_S0_mmmmS1_S1_",
+                                     [_HP, _IP, _IP, _HP, _IP, _IP, C.c_void_p, _HP, _HP, _HP, _SZ, _SZ, _SZ, _SZ,
+                                      _IP, _IP]),
+    "preprocessing_mmaSTKernel": ("_Z25preprocessing_mmaSTKernelP6__halfPcS0_mmmmPiS2_",
+                                  [_HP, C.c_void_p, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+}
+
+
+def ref_shim(name):
+    """A reference launcher exported by libsmat, callable through ctypes."""
+    mangled, args = REF_SHIMS[name]
+    f = getattr(lib(), mangled)
+    f.restype = None
+    f.argtypes = args
+    return f
