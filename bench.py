@@ -375,15 +375,84 @@ def run_smat(args):
     M.close()
 
 
+FORMS_WORKLOAD = {
+    "workload": "stencil27_64cubed_N256",
+    "generator": "27-point stencil on a 64^3 grid, natural order, off-diagonal N(1,0.1), diagonal 27+N(0,1), FP32",
+    "block": [16, 16],
+    "N": 256,
+    "B": "262144x256 FP32 N(0,1), row-major",
+    "C": "FP32",
+    "l2": "no flush: B (268 MB FP32) and C (268 MB) exceed the 129 MB L2",
+}
+
+
+def run_forms(args):
+    """The precision forms on the stencil workload: one JSON line per form with
+    its useful TFLOP/s (pack B + contraction) and its error against FP64."""
+    import torch
+
+    import smat
+    from smat import generators as G
+    dev = torch.device("cuda", 0)
+    A = G.stencil27(64, seed=4)
+    N = FORMS_WORKLOAD["N"]
+    forms = {"f16": smat.FORM_F16, "bf16": smat.FORM_BF16, "fp8": smat.FORM_FP8, "split_bf16": smat.FORM_SPLIT_BF16}
+    t0 = time.time()
+    M = smat.Bcsr(A, forms=tuple(forms.values()))
+    log(f"[bench] stencil BCSR built in {time.time() - t0:.1f}s: {M.info}")
+    Bf = np.random.default_rng(7).standard_normal((A.cols, N)).astype(np.float32)
+    B = torch.from_numpy(Bf).to(dev)
+    Cd = torch.empty((A.rows, N), dtype=torch.float32, device=dev)
+    import scipy.sparse as sps
+    ref = sps.csr_matrix((A.values.astype(np.float64), A.col_idx, A.row_ptr), shape=(A.rows, A.cols)) @ \
+        Bf.astype(np.float64)
+    nrm = np.linalg.norm(ref)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    info = M.info
+    for name, f in forms.items():
+        ws_bytes = M.workspace_size(f, smat.F32, N)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+
+        def step():
+            M.spmm_raw(f, B, smat.F32, smat.ROW_MAJOR, N, Cd, smat.F32, N, N, ws, ws_bytes, sp)
+
+        step()
+        torch.cuda.synchronize(dev)
+        M.check_device_error()
+        err = float(np.linalg.norm(Cd.cpu().numpy().astype(np.float64) - ref) / nrm)
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        useful = 2.0 * A.nnz * N
+        print(json.dumps({"metric": METRIC, "form": name, "value": useful / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                          "ms_per_step": ms, "rel_err_vs_fp64": err, "steps": args.steps, "warmup": args.warmup,
+                          "higher_is_better": True, "data": "synthetic",
+                          "config": dict(FORMS_WORKLOAD, nnz=A.nnz, nnzb=info["nnzb"], fill=info["fill"],
+                                         panel_rows=info["panel_rows"])}), flush=True)
+        del ws
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="smat", choices=["smat", "reference"])
+    ap.add_argument("--workload", default="rmat16", choices=["rmat16", "stencil64_forms"],
+                    help="rmat16: the headline SpMM line; stencil64_forms: one line per precision form")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "stencil64_forms":
+        run_forms(args)
     else:
         run_smat(args)
 

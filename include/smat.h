@@ -174,6 +174,12 @@ smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info);
 smat_status smat_bcsr_export(const smat_bcsr* A, int32_t* row_ptr, int32_t* col_idx,
                              uint16_t* values_f16, uint8_t* is_24);
 
+/* The FP8 form's data, BCSR block order: codes[nnzb*256] e4m3 (OCP "e4m3fn")
+ * codes of value / scale, row-major per block, and scales[nnzb]; the SpMM
+ * uses FP16(code value * scale). Each block's scale is chosen on the host to
+ * minimise the block's squared quantisation error. */
+smat_status smat_bcsr_export_fp8(const smat_bcsr* A, uint8_t* codes, float* scales);
+
 /* Host-only CSR -> BCSR (no device needed): the block structure that
  * smat_bcsr_create uploads, bit-identical to SparseMatrix::csrToBcsr
  * (matrix.h:666-792) on the (optionally permuted) CSR. Call once with
@@ -237,6 +243,89 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
 smat_status smat_spmm_static_scratch(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
                                      int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,
                                      int64_t N, void* stream);
+
+/* ---------------------------------------------------------------- autotuner */
+
+typedef struct smat_tune_result {
+  int32_t panel_rows;   /* block rows per panel that measured fastest */
+  float split_frac;     /* panel splitting threshold that measured fastest (< 0: none) */
+  double ms;            /* its SpMM time (pack B + contraction), milliseconds */
+  double ms_default;    /* the default shape's time, for comparison (0 if cached) */
+  int32_t cached;       /* 1: answered from the cache without measuring */
+} smat_tune_result;
+
+/* Measures the launch shapes offered for A (block rows per panel, and the
+ * panel-splitting threshold) for this form and N on opts->device, and keeps
+ * the fastest in a process-wide cache keyed on A's block-density statistics
+ * (blocks per block row, blocks per B tile in a 16-row panel), the N-tile
+ * count and the form's kernel. Later smat_bcsr_create calls with
+ * panel_rows = 0 use the cached shape for matrices with the same key. No
+ * counterpart in the reference (its tile shape is fixed at compile time).
+ * Allocates device memory for its trial runs and synchronises. */
+smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t form, int64_t N,
+                          smat_tune_result* out);
+smat_status smat_autotune_clear(void);
+
+/* 64 values describing A for the tau / block-shape predictor, computed on
+ * `device`: a row-length histogram, a bandwidth profile, the fill histogram
+ * of the nonzero 16 x 16 tiles and scalar statistics (layout in
+ * sptc-smat_gb300/csrc/features.cu). No counterpart in the reference. */
+smat_status smat_features(const smat_csr* A, int32_t device, float* out64);
+
+/* ------------------------------------------------- learned tau / block choice */
+
+/* A 64-128-128-12 FP32 MLP (ReLU hidden layers) predicting, from
+ * smat_features, the reordering threshold tau in {0.1, ..., 0.9} (logits
+ * 0..8) and the block shape {8x8, 16x16, 32x16} (logits 9..11); trained with
+ * the sum of the two heads' softmax cross-entropies and Adam, forward,
+ * backward and update all in libsmat's own kernels. Inputs and outputs are
+ * host arrays. No counterpart in the reference. */
+typedef struct smat_mlp smat_mlp;
+smat_status smat_mlp_create(int32_t device, uint64_t seed, smat_mlp** out);
+int32_t smat_mlp_num_params(void);
+smat_status smat_mlp_get_params(const smat_mlp* m, float* params);
+smat_status smat_mlp_set_params(smat_mlp* m, const float* params);
+/* Loss and gradient (parameter layout as the parameters) of one batch. */
+smat_status smat_mlp_gradients(smat_mlp* m, const float* X, const int32_t* y_tau, const int32_t* y_block,
+                               int32_t batch, float* grads, float* loss);
+/* One Adam step (lr, beta 0.9 / 0.999, eps 1e-8) on one batch. */
+smat_status smat_mlp_train_step(smat_mlp* m, const float* X, const int32_t* y_tau, const int32_t* y_block,
+                                int32_t batch, float lr, float* loss);
+smat_status smat_mlp_predict(smat_mlp* m, const float* X, int32_t batch, float* logits);
+smat_status smat_mlp_destroy(smat_mlp* m);
+
+/* ---------------------------------------------------------------- groups */
+
+/* One SpMM of a group: C = A * B with the arguments of smat_spmm. */
+typedef struct smat_problem {
+  const smat_bcsr* A;
+  int32_t form;
+  const void* B;      /* (device) */
+  int32_t b_dtype;
+  int32_t b_layout;
+  int64_t ldb;
+  void* C;            /* (device) */
+  int32_t c_dtype;
+  int64_t ldc;
+  int64_t N;
+} smat_problem;
+
+typedef struct smat_group smat_group;
+
+/* Many SpMMs of uneven sizes in one persistent launch (no counterpart in the
+ * reference, which runs one matrix at a time). smat_group_create builds, once,
+ * one load-balanced work list over all the problems' block-row panels, their
+ * descriptors and scratch (device memory owned by the group); B and C
+ * pointers are fixed here. All handles must be on one device. */
+smat_status smat_group_create(const smat_problem* problems, int32_t count, smat_group** out);
+/* Runs the group on `stream`: one grouped B-packing launch, one counter
+ * clear, one SpMM launch per kernel variant among the problems (one for
+ * FP16/BF16 problems with N <= 128). Allocates and synchronises nothing, so
+ * it can be captured in a CUDA graph (after a first run outside capture). */
+smat_status smat_group_run(smat_group* g, void* stream);
+/* As smat_bcsr_check_device_error, for the group's launches. */
+smat_status smat_group_check_device_error(smat_group* g);
+smat_status smat_group_destroy(smat_group* g);
 
 /* Host-buffer variant: copies B (host) in, runs smat_spmm, copies C (host)
  * out, and waits for completion. Uses device buffers cached in the handle. */

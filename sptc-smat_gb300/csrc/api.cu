@@ -61,42 +61,6 @@ static smat_status upload(T** dptr, const T* src, size_t n) {
 
 using namespace smat;
 
-struct Sched {
-  int grid = 0;
-  int32_t* d_cta_ptr = nullptr;
-  int32_t* d_cta_items = nullptr;
-  WorkItem* d_items = nullptr;
-  int32_t n_split = 0;  // panels split into parts
-  int32_t n_slabs = 0;  // parts of split panels
-};
-
-struct smat_bcsr {
-  int device = 0;
-  HostBcsr host;
-  Plan plan;
-  uint32_t forms = 0;
-  int use24 = 0;
-  int64_t n_24 = 0;
-  int num_sms = 0;
-  int32_t* d_row_map = nullptr;
-  PanelInfo* d_panels = nullptr;
-  StageRec* d_stages = nullptr;
-  Sched sched[3];  // by NSUB (1, 2)
-  // A stream per form (F16, BF16, -, SPLIT): per stage the pre-swizzled
-  // blocks in consumption order (hi, then lo for the split form) and the
-  // stage header
-  uint8_t* d_aval[4] = {nullptr, nullptr, nullptr, nullptr};
-  int* d_err = nullptr;
-  // smat_spmm_host staging
-  std::mutex mu;
-  void* d_bstage = nullptr;
-  size_t bstage_bytes = 0;
-  void* d_cstage = nullptr;
-  size_t cstage_bytes = 0;
-  void* d_ws = nullptr;
-  size_t ws_bytes = 0;
-};
-
 static void free_handle(smat_bcsr* h) {
   if (!h) return;
   int prev = -1;
@@ -112,8 +76,13 @@ static void free_handle(smat_bcsr* h) {
   delete h;
 }
 
-static int pick_nsub(const smat_bcsr* h, int64_t N, bool split) {
-  if (N > 128 && !split && tc_variant_supported(h->host.bh, h->plan.R, 2, split)) return 2;
+// Kernel kind of an arithmetic form.
+int smat::kind_of(int32_t form) {
+  return form == SMAT_FORM_SPLIT_BF16 ? TC_KIND_SPLIT : (form == SMAT_FORM_FP8 ? TC_KIND_FP8 : TC_KIND_PLAIN);
+}
+
+int smat::pick_nsub(const smat_bcsr* h, int64_t N, int kind) {
+  if (N > 128 && kind == TC_KIND_PLAIN && tc_variant_supported(h->host.bh, h->plan.R, 2, kind)) return 2;
   return 1;
 }
 
@@ -128,7 +97,19 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   // 16 block rows per panel (8 of 32 rows) fill TMEM's 512 columns with two
   // accumulator buffers; heavy panels are split over CTAs below
   int R = o.panel_rows ? o.panel_rows : (bh == 16 ? 16 : 8);
-  if (!tc_variant_supported(bh, R, 1, false)) {
+  float split_frac = o.split_frac;
+  if (o.panel_rows == 0) {
+    // a configuration the autotuner measured for matrices like this one
+    TuneKey key;
+    if (tune_key_of(h->host, kind_of(SMAT_FORM_F16), 128, key)) {
+      TuneVal tv;
+      if (tune_lookup(key, tv)) {
+        R = tv.panel_rows;
+        if (o.split_frac == 0.0f) split_frac = tv.split_frac;
+      }
+    }
+  }
+  if (!tc_variant_supported(bh, R, 1, TC_KIND_PLAIN)) {
     delete h;
     return fail(SMAT_ERR_UNSUPPORTED, "unsupported panel_rows for this block height");
   }
@@ -162,13 +143,13 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   // work items per launch shape (NSUB 1 and 2): heavy panels split into
   // parts so that no CTA gets much more than the average
   for (int nsub = 1; nsub <= 2; nsub++) {
-    if (!tc_variant_supported(bh, R, nsub, false)) continue;
-    const int per_sm = tc_ctas_per_sm(bh, R, nsub, false);
+    if (!tc_variant_supported(bh, R, nsub, TC_KIND_PLAIN)) continue;
+    const int per_sm = tc_ctas_per_sm(bh, R, nsub, TC_KIND_PLAIN);
     const int workers = std::max(1, h->num_sms * per_sm);
     std::vector<WorkItem> items;
     std::vector<int32_t> cta_ptr, cta_items;
     Sched& sc = h->sched[nsub];
-    const double frac = o.split_frac == 0.0f ? 1.0 : (o.split_frac < 0.0f ? 1e30 : (double)o.split_frac);
+    const double frac = split_frac == 0.0f ? 1.0 : (split_frac < 0.0f ? 1e30 : (double)split_frac);
     build_work_items(pl, bh, workers, frac, items, cta_ptr, cta_items, sc.n_split, sc.n_slabs);
     sc.grid = std::max(1, std::min<int>(workers, (int)items.size()));
     cta_ptr.resize(sc.grid + 1);  // queues past the item count are empty
@@ -226,6 +207,31 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
       stream_layout(hi, &lo, lay);
       SMAT_TRY(upload(&h->d_aval[SMAT_FORM_SPLIT_BF16], lay.data(), lay.size()));
     }
+  }
+  if (forms & (1u << SMAT_FORM_FP8)) {
+    if (bh != 16) {
+      free_handle(h);
+      return fail(SMAT_ERR_UNSUPPORTED, "FP8 form: 16 x 16 blocks only");
+    }
+    SMAT_TRY(quantize_fp8(b, h->fp8_q, h->fp8_scale));
+    // per stage: [nblk e4m3 blocks][nblk FP32 scales, padded][header]
+    lay.assign(std::max<size_t>((size_t)nnzb * 256 + pl.headers.size() +
+                                    (nst ? (size_t)pl.stages[nst - 1].scl_off + fp8_scale_bytes(pl.stages[nst - 1].nblk) : 0),
+                                16),
+               0);
+#pragma omp parallel for schedule(static)
+    for (int64_t si = 0; si < nst; si++) {
+      const StageRec& r = pl.stages[si];
+      uint8_t* base = lay.data() + (size_t)r.blk_off * 256 + (size_t)r.scl_off + (size_t)r.hdr_off;
+      for (int32_t qb = 0; qb < r.nblk; qb++) {
+        const int64_t blk = pl.stream_blk[r.blk_off + qb];
+        std::memcpy(base + (size_t)qb * 256, h->fp8_q.data() + (size_t)blk * 256, 256);
+        std::memcpy(base + (size_t)r.nblk * 256 + (size_t)qb * 4, &h->fp8_scale[blk], 4);
+      }
+      std::memcpy(base + (size_t)r.nblk * 256 + fp8_scale_bytes(r.nblk), pl.headers.data() + r.hdr_off,
+                  (size_t)r.hdr_bytes);
+    }
+    SMAT_TRY(upload(&h->d_aval[SMAT_FORM_FP8], lay.data(), lay.size()));
   }
   // keep the FP16 values for export; the FP32 copy is no longer needed
   std::vector<float>().swap(h->host.val);
@@ -307,7 +313,6 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
   if (bw != 16 || (bh != 16 && bh != 32))
     return fail(SMAT_ERR_UNSUPPORTED, "tensor-core path supports 16x16 and 32x16 blocks");
   const uint32_t forms = o.forms ? o.forms : (1u << SMAT_FORM_F16);
-  if (forms & (1u << SMAT_FORM_FP8)) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
   smat_bcsr* h = nullptr;
   smat_status st = new_handle(o, forms, &h);
   if (st != SMAT_OK) return st;
@@ -329,7 +334,6 @@ smat_status smat_bcsr_create_from_bcsr(int64_t rows, int64_t cols, int32_t block
   if (opts) o = *opts;
   if (o.row_perm) return fail(SMAT_ERR_UNSUPPORTED, "row_perm applies to CSR input only");
   const uint32_t forms = o.forms ? o.forms : (1u << SMAT_FORM_F16);
-  if (forms & (1u << SMAT_FORM_FP8)) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
   smat_bcsr* h = nullptr;
   smat_status st = new_handle(o, forms, &h);
   if (st != SMAT_OK) return st;
@@ -344,6 +348,14 @@ smat_status smat_bcsr_create_from_bcsr(int64_t rows, int64_t cols, int32_t block
 
 smat_status smat_bcsr_destroy(smat_bcsr* A) {
   free_handle(A);
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_export_fp8(const smat_bcsr* A, uint8_t* codes, float* scales) {
+  if (!A) return fail(SMAT_ERR_INVALID, "null handle");
+  if (!(A->forms & (1u << SMAT_FORM_FP8))) return fail(SMAT_ERR_INVALID, "FP8 form was not materialised");
+  if (codes) std::copy(A->fp8_q.begin(), A->fp8_q.end(), codes);
+  if (scales) std::copy(A->fp8_scale.begin(), A->fp8_scale.end(), scales);
   return SMAT_OK;
 }
 
@@ -396,18 +408,14 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
   return SMAT_OK;
 }
 
-// Workspace layout of one SpMM: [packed B (x2 for the split form)]
-// [per split panel, column tile and TMEM lane quadrant: an int counter]
-// [per part of a split panel and column tile: an R*bh x BN FP32 slab].
-struct WsLayout {
-  size_t counters = 0, counter_bytes = 0, slabs = 0, total = 0;
-};
-static WsLayout ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
+}  // extern "C"
+
+WsLayout smat::ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
   WsLayout w;
   const bool split = form == SMAT_FORM_SPLIT_BF16;
   const size_t one = (packed_b_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
   w.counters = split ? 2 * one : one;
-  const int nsub = pick_nsub(A, N, split);
+  const int nsub = pick_nsub(A, N, kind_of(form));
   const Sched& sc = A->sched[nsub];
   const int64_t bn = 128 * nsub, n_tiles = (std::max<int64_t>(N, 1) + bn - 1) / bn;
   w.counter_bytes = ((size_t)sc.n_split * n_tiles * 4 * sizeof(int32_t) + 255) / 256 * 256;
@@ -415,6 +423,35 @@ static WsLayout ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
   w.total = w.slabs + (size_t)sc.n_slabs * n_tiles * A->plan.R * A->host.bh * bn * sizeof(float);
   return w;
 }
+
+// The kernel's view of one SpMM: A's device plan and stream for the form,
+// the packed B and scratch at `ws` (laid out as ws_layout), C.
+void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64_t N, void* C, int32_t c_dtype,
+                        int64_t ldc, int nsub, const WsLayout& wl, ProblemDesc& P) {
+  std::memset(&P, 0, sizeof(P));
+  uint8_t* ws = const_cast<uint8_t*>(static_cast<const uint8_t*>(ws_));
+  const int64_t bn = 128 * nsub;
+  P.bpack = ws;
+  P.bp_ntiles = packed_b_tiles(N);
+  P.aval = A->d_aval[form];
+  P.panels = A->d_panels;
+  P.stages = A->d_stages;
+  P.row_map = A->d_row_map;
+  P.C = C;
+  P.ldc = ldc;
+  P.counters = reinterpret_cast<int32_t*>(ws + wl.counters);
+  P.slabs = reinterpret_cast<float*>(ws + wl.slabs);
+  P.N = (int32_t)N;
+  P.n_tiles = (int32_t)((N + bn - 1) / bn);
+  P.nbr = (int32_t)A->host.nbr();
+  P.c_f16 = c_dtype == SMAT_F16;
+  // instruction descriptor (kind::f16): FP32 accumulator, FP16 (0) or BF16 (1)
+  // operands, both K-major, M = 128; the kernel adds N per MMA group
+  const uint32_t fmt = (form == SMAT_FORM_F16 || form == SMAT_FORM_FP8) ? 0u : 1u;
+  P.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(128 >> 4) << 24);
+}
+
+extern "C" {
 
 smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
                                      size_t* bytes) {
@@ -428,7 +465,6 @@ static smat_status check_common(const smat_bcsr* A, int32_t form, int64_t N) {
   if (!A) return fail(SMAT_ERR_INVALID, "null handle");
   if (form < 0 || form > 3 || !(A->forms & (1u << form)))
     return fail(SMAT_ERR_INVALID, "form was not materialised when the handle was built");
-  if (form == SMAT_FORM_FP8) return fail(SMAT_ERR_UNSUPPORTED, "FP8 form not built yet");
   if (N <= 0 || N > (1 << 30)) return fail(SMAT_ERR_INVALID, "bad N");
   return SMAT_OK;
 }
@@ -454,7 +490,7 @@ smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, in
   const bool split = form == SMAT_FORM_SPLIT_BF16;
   uint8_t* out = static_cast<uint8_t*>(workspace);
   const int in_dt = b_dtype == SMAT_F32 ? 0 : (b_dtype == SMAT_F16 ? 1 : 2);
-  const int mode = form == SMAT_FORM_F16 ? 0 : (split ? 2 : 1);
+  const int mode = (form == SMAT_FORM_F16 || form == SMAT_FORM_FP8) ? 0 : (split ? 2 : 1);
   cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, out, K, N,
                          static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "pack_b");
@@ -472,44 +508,25 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   if (hb.rows == 0) return SMAT_OK;
   DeviceGuard guard(A->device);
   if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
-  const bool split = form == SMAT_FORM_SPLIT_BF16;
-  const int nsub = pick_nsub(A, N, split);
+  const int kind = kind_of(form);
+  const int nsub = pick_nsub(A, N, kind);
   const int bh = hb.bh, R = A->plan.R;
-  if (!tc_variant_supported(bh, R, nsub, split)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
+  if (!tc_variant_supported(bh, R, nsub, kind)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
   const Sched& sc = A->sched[nsub];
   SpmmArgs args;
   std::memset(&args, 0, sizeof(args));
-  const uint32_t BN = 128u * nsub;
-  args.bpack = static_cast<const uint8_t*>(packed_b);
-  args.bp_ntiles = packed_b_tiles(N);
-  args.aval = A->d_aval[form];
-  args.panels = A->d_panels;
-  args.stages = A->d_stages;
+  const WsLayout wl = ws_layout(A, form, N);
+  fill_problem(A, form, packed_b, N, C, c_dtype, ldc, nsub, wl, args.one);
   args.cta_ptr = sc.d_cta_ptr;
   args.cta_items = sc.d_cta_items;
   args.items = sc.d_items;
-  const WsLayout wl = ws_layout(A, form, N);
-  uint8_t* ws = const_cast<uint8_t*>(static_cast<const uint8_t*>(packed_b));
-  args.counters = reinterpret_cast<int32_t*>(ws + wl.counters);
-  args.slabs = reinterpret_cast<float*>(ws + wl.slabs);
+  args.err = A->d_err;
   if (sc.n_split > 0) {
     // the split panels' counters start at zero in every launch
-    cudaError_t e = cudaMemsetAsync(args.counters, 0, wl.counter_bytes, static_cast<cudaStream_t>(stream_));
+    cudaError_t e = cudaMemsetAsync(args.one.counters, 0, wl.counter_bytes, static_cast<cudaStream_t>(stream_));
     if (e != cudaSuccess) return cuda_fail(e, "clearing the split-panel counters");
   }
-  args.row_map = A->d_row_map;
-  args.C = C;
-  args.ldc = ldc;
-  args.N = (int32_t)N;
-  args.n_tiles = (int32_t)((N + BN - 1) / BN);
-  args.nbr = (int32_t)hb.nbr();
-  args.c_f16 = c_dtype == SMAT_F16;
-  // instruction descriptor (kind::f16): FP32 accumulator, FP16 (0) or BF16 (1)
-  // operands, both K-major, M = 128; the kernel adds N per MMA group
-  const uint32_t fmt = (form == SMAT_FORM_F16) ? 0u : 1u;
-  args.idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(128 >> 4) << 24);
-  args.err = A->d_err;
-  cudaError_t e = tc_launch(bh, R, nsub, split, args, sc.grid, static_cast<cudaStream_t>(stream_));
+  cudaError_t e = tc_launch(bh, R, nsub, kind, args, sc.grid, static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "spmm kernel launch");
   return SMAT_OK;
 }

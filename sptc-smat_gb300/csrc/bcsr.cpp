@@ -224,6 +224,58 @@ smat_status build_host_bcsr_from_blocks(int64_t rows, int64_t cols, int32_t bh, 
   return SMAT_OK;
 }
 
+// Nearest e4m3 value (round to nearest even) of a in [0, 464).
+static inline float e4m3_round(float a) {
+  if (a < 0.015625f) return std::nearbyint(a * 512.0f) * (1.0f / 512.0f);  // subnormals: step 2^-9
+  uint32_t bits;
+  std::memcpy(&bits, &a, 4);
+  const int e = (int)((bits >> 23) & 0xffu) - 127;                          // a in [2^e, 2^(e+1))
+  const uint32_t step_bits = (uint32_t)(e - 3 + 127) << 23;                  // 2^(e-3): 3 fraction bits
+  float step;
+  std::memcpy(&step, &step_bits, 4);
+  return std::min(448.0f, std::nearbyint(a / step) * step);
+}
+
+smat_status quantize_fp8(const HostBcsr& b, std::vector<uint8_t>& q, std::vector<float>& scale) {
+  const int64_t nnzb = b.nnzb();
+  const int bsz = b.bh * b.bw;
+  for (float v : b.val)
+    if (!(std::fabs(v) <= 65504.0f))
+      return fail(SMAT_ERR_UNSUPPORTED, "FP8 form: values must be finite and within the FP16 range");
+  q.assign((size_t)nnzb * bsz, 0);
+  scale.assign(nnzb, 1.0f);
+  // candidate maps of the block's largest magnitude: 448 down to 224 (one
+  // binade), so that some scale puts the block's values on a good e4m3 grid
+  constexpr int kCand = 24;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t k = 0; k < nnzb; k++) {
+    const float* v = b.val.data() + (size_t)k * bsz;
+    float amax = 0.0f;
+    for (int i = 0; i < bsz; i++) amax = std::max(amax, std::fabs(v[i]));
+    if (amax == 0.0f) continue;
+    float best_s = amax / 448.0f;
+    double best_e = INFINITY;
+    for (int c = 0; c < kCand; c++) {
+      const float t = 448.0f - 224.0f * (float)c / (float)kCand;
+      const float sc = amax / t;
+      double e = 0.0;
+      for (int i = 0; i < bsz; i++) {
+        if (v[i] == 0.0f) continue;
+        const float r = e4m3_round(std::fabs(v[i]) / sc) * sc;
+        const double d = (double)r - (double)std::fabs(v[i]);
+        e += d * d;
+      }
+      if (e < best_e) {
+        best_e = e;
+        best_s = sc;
+      }
+    }
+    scale[k] = best_s;
+    for (int i = 0; i < bsz; i++) q[(size_t)k * bsz + i] = v[i] == 0.0f ? 0 : f32_to_e4m3_bits(v[i] / best_s);
+  }
+  return SMAT_OK;
+}
+
 smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
   if (R < 1 || R > 32) return fail(SMAT_ERR_INVALID, "panel rows must be in [1, 32]");
   const int64_t nbr = b.nbr();
@@ -342,14 +394,15 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
     nb += (int64_t)L.blk.size();
     nh += (int64_t)L.hdr.size();
   }
-  if (nst >= ((int64_t)1 << 31)) return fail(SMAT_ERR_UNSUPPORTED, "plan too large");
+  if (nst >= ((int64_t)1 << 31) || (int64_t)nb * 4 + nst * 16 >= ((int64_t)1 << 31))
+    return fail(SMAT_ERR_UNSUPPORTED, "plan too large");
   plan.panels.resize(P);
   plan.stages.resize(nst);
   plan.stream_blk.resize(nb);
   plan.headers.resize(nh);
   plan.n_groups = 0;
   plan.n_tiles = 0;
-  int64_t so = 0, bo = 0, ho = 0;
+  int64_t so = 0, bo = 0, ho = 0, xo = 0;
   for (int32_t p = 0; p < P; p++) {
     Local& L = loc[p];
     L.info.stage_off = (int32_t)so;
@@ -360,8 +413,10 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
       StageRec r = L.stages[c];
       r.blk_off = bo;
       r.hdr_off = ho;
+      r.scl_off = (int32_t)xo;
       bo += r.nblk;
       ho += r.hdr_bytes;
+      xo += fp8_scale_bytes(r.nblk);
       plan.stages[so + c] = r;
     }
     so += (int64_t)L.stages.size();
@@ -371,61 +426,91 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
   return SMAT_OK;
 }
 
-void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
-                      std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
-                      std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs) {
+void build_work_items_multi(const std::vector<const Plan*>& plans, const std::vector<int32_t>& bhs, int32_t workers,
+                            double max_item_frac, std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
+                            std::vector<int32_t>& cta_items, std::vector<int32_t>& n_split,
+                            std::vector<int32_t>& n_slabs) {
   // cost of a stage in units of one A block: the block copies, the B tiles
   // (a 4 KB tile moves 8x the bytes of a block, from L2) and a fixed
   // per-stage hand-off cost; per item, the epilogue (R * bh rows of C)
-  const int32_t P = pl.n_panels;
-  auto stage_cost = [&](const StageRec& r) { return r.nblk + 2.0 * r.ntiles + 4.0; };
-  std::vector<double> pcost(P, 0.0);
+  auto stage_cost = [](const StageRec& r) { return r.nblk + 2.0 * r.ntiles + 4.0; };
+  const int32_t np = (int32_t)plans.size();
+  std::vector<std::vector<double>> pcost(np);
   double total = 0.0;
-  for (int32_t p = 0; p < P; p++) {
-    for (int32_t c = 0; c < pl.panels[p].nstages; c++) pcost[p] += stage_cost(pl.stages[pl.panels[p].stage_off + c]);
-    pcost[p] += 0.5 * pl.R * bh;
-    total += pcost[p];
+  for (int32_t q = 0; q < np; q++) {
+    const Plan& pl = *plans[q];
+    pcost[q].assign(pl.n_panels, 0.0);
+    for (int32_t p = 0; p < pl.n_panels; p++) {
+      for (int32_t c = 0; c < pl.panels[p].nstages; c++)
+        pcost[q][p] += stage_cost(pl.stages[pl.panels[p].stage_off + c]);
+      pcost[q][p] += 0.5 * pl.R * bhs[q];
+      total += pcost[q][p];
+    }
   }
-  const double max_item = std::max(1.0, max_item_frac * total / std::max(1, workers));
-  items.clear();
-  n_split = 0;
-  n_slabs = 0;
-  std::vector<double> icost;
-  for (int32_t p = 0; p < P; p++) {
-    const PanelInfo& pi = pl.panels[p];
-    int32_t parts = (int32_t)std::ceil(pcost[p] / max_item);
-    parts = std::max(1, std::min(parts, pi.nstages));
-    if (parts == 1) {
-      items.push_back(WorkItem{p, 0, pi.nstages, -1, 0, 1, 0, 0});
-      icost.push_back(pcost[p]);
-      continue;
-    }
-    // cut the stages into `parts` ranges of about equal cost
-    const double per = (pcost[p] - 0.5 * pl.R * bh) / parts;
-    int32_t s0 = 0;
-    double acc = 0.0;
-    int32_t part = 0;
-    for (int32_t c = 0; c < pi.nstages; c++) {
-      acc += stage_cost(pl.stages[pi.stage_off + c]);
-      const bool cut = acc >= per * (part + 1) && part < parts - 1 && c + 1 < pi.nstages;
-      if (cut || c + 1 == pi.nstages) {
-        items.push_back(WorkItem{p, s0, c + 1, n_split, part, 0, n_slabs, 0});
-        part++;
-        s0 = c + 1;
+  double max_item = std::max(1.0, max_item_frac * total / std::max(1, workers));
+  // bound the partial-sum slabs: at most kMaxSlabs parts of split panels per
+  // problem (coarser parts where a problem would need more)
+  constexpr int64_t kMaxSlabs = 96;
+  for (int32_t q = 0; q < np; q++) {
+    for (int iter = 0; iter < 64; iter++) {
+      int64_t parts_q = 0;
+      for (int32_t p = 0; p < plans[q]->n_panels; p++) {
+        const int64_t parts = std::min<int64_t>((int64_t)std::ceil(pcost[q][p] / max_item), plans[q]->panels[p].nstages);
+        if (parts > 1) parts_q += parts;
       }
+      if (parts_q <= kMaxSlabs) break;
+      max_item *= 1.25;
     }
-    const int32_t made = part;
-    for (int32_t i = (int32_t)items.size() - made; i < (int32_t)items.size(); i++) {
-      items[i].nparts = made;
-      double c = 0.0;
-      for (int32_t st = items[i].s0; st < items[i].s1; st++) c += stage_cost(pl.stages[pi.stage_off + st]);
-      // a part writes its slab; the last one also reads all parts back
-      icost.push_back(c + 0.5 * pl.R * bh * 2);
+  }
+  items.clear();
+  n_split.assign(np, 0);
+  n_slabs.assign(np, 0);
+  std::vector<double> icost;
+  for (int32_t q = 0; q < np; q++) {
+    const Plan& pl = *plans[q];
+    const double epi = 0.5 * pl.R * bhs[q];
+    for (int32_t p = 0; p < pl.n_panels; p++) {
+      const PanelInfo& pi = pl.panels[p];
+      int32_t parts = (int32_t)std::ceil(pcost[q][p] / max_item);
+      parts = std::max(1, std::min(parts, pi.nstages));
+      if (parts == 1) {
+        items.push_back(WorkItem{p, 0, pi.nstages, -1, 0, 1, 0, q});
+        icost.push_back(pcost[q][p]);
+        continue;
+      }
+      // cut the stages into `parts` ranges of about equal cost
+      const double per = (pcost[q][p] - epi) / parts;
+      int32_t s0 = 0, part = 0;
+      double acc = 0.0;
+      for (int32_t c = 0; c < pi.nstages; c++) {
+        acc += stage_cost(pl.stages[pi.stage_off + c]);
+        const bool cut = acc >= per * (part + 1) && part < parts - 1 && c + 1 < pi.nstages;
+        if (cut || c + 1 == pi.nstages) {
+          items.push_back(WorkItem{p, s0, c + 1, n_split[q], part, 0, n_slabs[q], q});
+          part++;
+          s0 = c + 1;
+        }
+      }
+      for (int32_t i = (int32_t)items.size() - part; i < (int32_t)items.size(); i++) {
+        items[i].nparts = part;
+        double c = 0.0;
+        for (int32_t st = items[i].s0; st < items[i].s1; st++) c += stage_cost(pl.stages[pi.stage_off + st]);
+        icost.push_back(c + 2.0 * epi);  // a part writes its slab; the last one also reads all parts back
+      }
+      n_split[q]++;
+      n_slabs[q] += part;
     }
-    n_split++;
-    n_slabs += made;
   }
   assign_items(icost, workers, cta_ptr, cta_items);
+}
+
+void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
+                      std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
+                      std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs) {
+  std::vector<int32_t> ns, nl;
+  build_work_items_multi({&pl}, {bh}, workers, max_item_frac, items, cta_ptr, cta_items, ns, nl);
+  n_split = ns[0];
+  n_slabs = nl[0];
 }
 
 void assign_items(const std::vector<double>& cost, int32_t workers, std::vector<int32_t>& cta_ptr,

@@ -65,11 +65,8 @@ __device__ __forceinline__ float vec_elem<__nv_bfloat16>(const uint4* v, int i) 
 // column-major layout the 16 k-values of a thread are contiguous and are
 // read as 16-byte vectors where they are aligned and inside K.
 template <typename T, int OUT>
-__global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ out,
-                             int64_t K, int64_t N, int ntiles) {
-  const int64_t kb = blockIdx.y;
-  const int t = blockIdx.x;
-  const int r = threadIdx.x;
+__device__ __forceinline__ void pack_tile(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ out,
+                                          int64_t K, int64_t N, int ntiles, int64_t kb, int t, int r) {
   const int64_t n = (int64_t)t * 128 + r;
   constexpr int VEC = 16 / sizeof(T);  // elements per 16-byte vector
   float xv[16];
@@ -113,6 +110,40 @@ __global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, 
 }
 
 template <typename T, int OUT>
+__global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ out,
+                             int64_t K, int64_t N, int ntiles) {
+  pack_tile<T, OUT>(in, layout, ldi, out, K, N, ntiles, blockIdx.y, blockIdx.x, threadIdx.x);
+}
+
+// Many B operands in one launch: block g packs tile (kb, t) of the job whose
+// block range holds g (jobs sorted by their first block).
+__global__ void pack_b_grouped_kernel(const PackJob* __restrict__ jobs, int njobs, int64_t total) {
+  for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].begin <= g) lo = mid; else hi = mid - 1;
+    }
+    const PackJob& j = jobs[lo];
+    const int64_t local = g - j.begin;
+    const int64_t kb = local / j.ntiles;
+    const int t = (int)(local % j.ntiles);
+#define SMAT_GPACK(T)                                                                                        \
+  switch (j.out_mode) {                                                                                      \
+    case OUT_F16: pack_tile<T, OUT_F16>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x); break; \
+    case OUT_BF16: pack_tile<T, OUT_BF16>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x); break; \
+    default: pack_tile<T, OUT_SPLIT>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x); break; \
+  }
+    switch (j.in_dtype) {
+      case 0: SMAT_GPACK(float) break;
+      case 1: SMAT_GPACK(__half) break;
+      default: SMAT_GPACK(__nv_bfloat16) break;
+    }
+#undef SMAT_GPACK
+  }
+}
+
+template <typename T, int OUT>
 static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* out, int64_t K, int64_t N,
                             cudaStream_t s) {
   const int ntiles = (int)packed_b_tiles(N);
@@ -151,6 +182,18 @@ cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int ou
     default: return cudaErrorInvalidValue;
   }
 #undef SMAT_PACK
+}
+
+}  // namespace smat
+
+namespace smat {
+
+cudaError_t pack_b_grouped(const PackJob* d_jobs, int njobs, int64_t total_blocks, int num_sms, cudaStream_t s) {
+  if (njobs == 0 || total_blocks == 0) return cudaSuccess;
+  const int64_t want = (int64_t)num_sms * 16;
+  const int grid = (int)(total_blocks < want ? total_blocks : want);
+  dev::pack_b_grouped_kernel<<<grid, 128, 0, s>>>(d_jobs, njobs, total_blocks);
+  return cudaGetLastError();
 }
 
 }  // namespace smat

@@ -22,4 +22,17 @@ size_t packed_b_bytes(int64_t K, int64_t N);
 cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* out,
                    int64_t K, int64_t N, cudaStream_t s);
 
+// One B operand of a grouped pack: tiles of `in` (in_dtype, layout, ldi,
+// K x N) into `out` (out_mode as pack_b), covering global blocks
+// [begin, begin + ntiles * ceil(K / 16)).
+struct PackJob {
+  const void* in;
+  uint8_t* out;
+  int64_t ldi, K, N, begin;
+  int32_t in_dtype, layout, out_mode, ntiles;
+};
+
+// Packs every job in one launch (jobs sorted by begin, in device memory).
+cudaError_t pack_b_grouped(const PackJob* d_jobs, int njobs, int64_t total_blocks, int num_sms, cudaStream_t s);
+
 }  // namespace smat

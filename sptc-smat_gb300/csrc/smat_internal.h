@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -77,6 +78,11 @@ struct Plan {
 
 smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);
 
+// FP8 form: per block (BCSR order) the e4m3 codes of value / scale and one
+// FP32 scale, chosen among candidates mapping the block's largest magnitude
+// to 448 ... 224 to minimise the block's squared quantisation error.
+smat_status quantize_fp8(const HostBcsr& b, std::vector<uint8_t>& q, std::vector<float>& scale);
+
 // Work items of one launch shape: panels whose cost exceeds max_item_frac
 // of the per-worker average are split into parts (stage ranges) of about
 // that size; the items are then assigned to `workers` queues. n_split =
@@ -85,6 +91,103 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);
 void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
                       std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
                       std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs);
+
+
+// ------------------------------------------------------------------ handle
+// Work list of one launch shape (NSUB).
+struct Sched {
+  int grid = 0;
+  int32_t* d_cta_ptr = nullptr;
+  int32_t* d_cta_items = nullptr;
+  WorkItem* d_items = nullptr;
+  int32_t n_split = 0;  // panels split into parts
+  int32_t n_slabs = 0;  // parts of split panels
+};
+
+struct SmatBcsrBody {
+  int device = 0;
+  HostBcsr host;
+  Plan plan;
+  uint32_t forms = 0;
+  int use24 = 0;
+  int64_t n_24 = 0;
+  int num_sms = 0;
+  int32_t* d_row_map = nullptr;
+  PanelInfo* d_panels = nullptr;
+  StageRec* d_stages = nullptr;
+  Sched sched[3];  // by NSUB (1, 2)
+  // A stream per form (F16, BF16, -, SPLIT): per stage the pre-swizzled
+  // blocks in consumption order (hi, then lo for the split form) and the
+  // stage header
+  uint8_t* d_aval[4] = {nullptr, nullptr, nullptr, nullptr};
+  // FP8 form, BCSR block order: e4m3 codes and per-block scales (for export)
+  std::vector<uint8_t> fp8_q;
+  std::vector<float> fp8_scale;
+  int* d_err = nullptr;
+  // smat_spmm_host staging
+  std::mutex mu;
+  void* d_bstage = nullptr;
+  size_t bstage_bytes = 0;
+  void* d_cstage = nullptr;
+  size_t cstage_bytes = 0;
+  void* d_ws = nullptr;
+  size_t ws_bytes = 0;
+};
+
+
+}  // namespace smat (the handle type is declared in the global namespace by smat.h)
+
+struct smat_bcsr : smat::SmatBcsrBody {};
+
+namespace smat {
+
+// Kernel kind of an arithmetic form, and the N-tile width (128 * nsub) used for N.
+int kind_of(int32_t form);
+int pick_nsub(const smat_bcsr* h, int64_t N, int kind);
+
+// Workspace layout of one SpMM: [packed B (x2 for the split form)]
+// [per split panel, column tile and TMEM lane quadrant: an int counter]
+// [per part of a split panel and column tile: an R*bh x BN FP32 slab].
+struct WsLayout {
+  size_t counters = 0, counter_bytes = 0, slabs = 0, total = 0;
+};
+WsLayout ws_layout(const smat_bcsr* A, int32_t form, int64_t N);
+
+// The kernel's view of one SpMM: A's device plan and stream for the form,
+// the packed B and scratch at `ws` (laid out as wl), C.
+void fill_problem(const smat_bcsr* A, int32_t form, const void* ws, int64_t N, void* C, int32_t c_dtype,
+                  int64_t ldc, int nsub, const WsLayout& wl, ProblemDesc& P);
+
+// The same over several problems (WorkItem::prob = index into plans); the
+// split decisions use the total over all problems; n_split / n_slabs per
+// problem.
+void build_work_items_multi(const std::vector<const Plan*>& plans, const std::vector<int32_t>& bhs, int32_t workers,
+                            double max_item_frac, std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
+                            std::vector<int32_t>& cta_items, std::vector<int32_t>& n_split,
+                            std::vector<int32_t>& n_slabs);
+
+// ------------------------------------------------------------------ autotuner
+// Key of the tuning cache: block-density statistics of a matrix (blocks per
+// block row and blocks per B tile of a 16-row panel, log2-bucketed), the
+// N-tile count and the kernel kind.
+struct TuneKey {
+  int32_t bh = 16, bpr_bucket = 0, reuse_bucket = 0, ntile_bucket = 0, kind = 0;
+  bool operator<(const TuneKey& o) const {
+    if (bh != o.bh) return bh < o.bh;
+    if (bpr_bucket != o.bpr_bucket) return bpr_bucket < o.bpr_bucket;
+    if (reuse_bucket != o.reuse_bucket) return reuse_bucket < o.reuse_bucket;
+    if (ntile_bucket != o.ntile_bucket) return ntile_bucket < o.ntile_bucket;
+    return kind < o.kind;
+  }
+};
+struct TuneVal {
+  int32_t panel_rows = 16;
+  float split_frac = 1.0f;
+  double ms = 0.0;
+};
+bool tune_key_of(const HostBcsr& b, int kind, int64_t N, TuneKey& key);
+bool tune_lookup(const TuneKey& key, TuneVal& val);
+void tune_store(const TuneKey& key, const TuneVal& val);
 
 // Longest-processing-time assignment of items to `workers` queues.
 void assign_items(const std::vector<double>& item_cost, int32_t workers,

@@ -45,6 +45,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "spmm_tc.h"
@@ -53,7 +54,7 @@
 namespace smat {
 namespace dev {
 
-enum : int { KIND_PLAIN = 0, KIND_SPLIT = 1 };
+enum : int { KIND_PLAIN = 0, KIND_SPLIT = 1, KIND_FP8 = 2 };
 
 // Stages between the L2 prefetch of a stage's A region and its copy.
 constexpr int kPrefetchAhead = 8;
@@ -66,6 +67,7 @@ enum : int {
   ERR_MMA_A = 202,
   ERR_MMA_B = 203,
   ERR_EPI = 301,
+  ERR_CONV = 302,
   ERR_DRAIN = 401
 };
 
@@ -77,8 +79,14 @@ struct Cfg {
   static constexpr uint32_t ABLK = BH * 32;               // bytes of one A block (one operand)
   static constexpr uint32_t TILE = BN * 32;               // bytes of one B tile (one operand)
   static constexpr uint32_t TILEB = TILE * NOPS;          // bytes of one B tile slot
-  // stage: [A blocks hi | lo | header] [B tiles] [header offset word]
-  static constexpr uint32_t OFF_B = (SB * ABLK * NOPS + kStageHdrMax + 1023) / 1024 * 1024;
+  static constexpr bool FP8 = KIND == KIND_FP8;
+  // stage: [A blocks hi | lo | header] [B tiles] [header offset word]; the
+  // FP8 form lands [e4m3 blocks | scales | header] in a staging area after
+  // the A blocks, which the converter warps turn into FP16 A blocks
+  static constexpr uint32_t OFF_STG = SB * ABLK * NOPS;
+  static constexpr uint32_t STG_BYTES = FP8 ? (SB * 256 + fp8_scale_bytes(SB) + kStageHdrMax + 255) / 256 * 256 : 0;
+  static constexpr uint32_t A_END = FP8 ? OFF_STG + STG_BYTES : OFF_STG + kStageHdrMax;
+  static constexpr uint32_t OFF_B = (A_END + 1023) / 1024 * 1024;
   static constexpr uint32_t OFF_HW = OFF_B + kStageTiles * TILEB;
   static constexpr uint32_t STAGE = (OFF_HW + 16 + 1023) / 1024 * 1024;
   static constexpr uint32_t SMEM_AVAIL = 227 * 1024 - 2048;  // minus alignment slack and barriers
@@ -89,9 +97,10 @@ struct Cfg {
   static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
   static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
   static constexpr int NPROD = 8;                         // copy warps
-  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA);
+  static constexpr int NCONV = FP8 ? 4 : 0;               // FP8 converter warps (16..19)
+  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? NS : 0));
   static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 16;
-  static constexpr int THREADS = 512;
+  static constexpr int THREADS = 512 + 32 * NCONV;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
@@ -100,6 +109,7 @@ struct Cfg {
   static_assert(kStageTiles == NPROD, "one copy warp per tile slot");
   static_assert(NS_FIT >= 2, "two stages must fit");
   static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+  static_assert(!FP8 || (BH == 16 && NSUB == 1), "FP8 form: 16 x 16 blocks, 128-column tiles");
 };
 
 // Wait used only while draining after an abort: bounded, ignores the flag.
@@ -130,7 +140,8 @@ __device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
 // Warp roles (16 warps): 0..3 MMA issuers (0 also owns TMEM), 4..7
 // epilogue (TMEM lane quadrants 0..3), 8..15 copy warps.
 template <int BH, int R, int NSUB, int KIND>
-__global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
+__global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
+    spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
   using C = Cfg<BH, R, NSUB, KIND>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -141,7 +152,8 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
   uint64_t* accfull = empty + C::NS;
   uint64_t* accempty = accfull + 2;
   uint64_t* drainbar = accempty + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drainbar + C::NMMA);
+  uint64_t* conv = drainbar + C::NMMA;  // FP8: the stage's A blocks are converted
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(conv + (C::FP8 ? C::NS : 0));
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
@@ -157,6 +169,8 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
       mbar_init(smem_u32(&accempty[i]), 4);
     }
     for (int i = 0; i < C::NMMA; i++) mbar_init(smem_u32(&drainbar[i]), 1);
+    if (C::FP8)
+      for (int i = 0; i < C::NS; i++) mbar_init(smem_u32(&conv[i]), C::NCONV);
     *abort_flag = 0;
     fence_barrier_init();
   }
@@ -171,11 +185,57 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
 
   const int it0 = args.cta_ptr[blockIdx.x];
   const int it1 = args.cta_ptr[blockIdx.x + 1];
-  const int n_tiles = args.n_tiles;
   int* err = args.err;
   const uint32_t smem0 = smem_u32(smem);
 
-  if (warp >= 8) {
+  if (C::FP8 && warp >= 16) {
+    // ------------------------------------------------------ FP8 converters
+    // Each stage's e4m3 blocks and FP32 scales land in the staging area;
+    // these four warps write them to the stage's A area as FP16 (value times
+    // its block's scale, one rounding) in the 32-byte-swizzled layout the
+    // MMA reads, make the writes visible to the tensor core's async proxy,
+    // and release the stage to the MMA warps (conv barrier).
+    const int ct = threadIdx.x - 512;
+    uint32_t ci = 0;
+    bool ok = true;
+    for (int it = it0; it < it1 && ok; ++it) {
+      const WorkItem wi = args.items[args.cta_items[it]];
+      const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+      const int n_tiles = P.n_tiles;
+      for (int nt = 0; nt < n_tiles && ok; ++nt) {
+        for (int c = wi.s0; c < wi.s1; ++c, ++ci) {
+          const uint32_t s = ci % C::NS;
+          if (!wait_phase(smem_u32(&full[s]), (ci / C::NS) & 1, abort_flag, err, ERR_CONV)) {
+            ok = false;
+            break;
+          }
+          uint8_t* stp = smem + s * C::STAGE;
+          const uint32_t hw = *reinterpret_cast<const uint32_t*>(stp + C::OFF_HW);
+          const int nblk = *reinterpret_cast<const uint16_t*>(stp + hw + 8);
+          const uint8_t* stg = stp + C::OFF_STG;
+          const float* scl = reinterpret_cast<const float*>(stg + nblk * 256);
+          for (int x = ct; x < nblk * 32; x += 128) {
+            const int b = x >> 5, r = (x >> 1) & 15, hh = x & 1;  // block, row, 8-column half
+            const uint2 raw = *reinterpret_cast<const uint2*>(stg + b * 256 + r * 16 + hh * 8);
+            const float sc = scl[b];
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const uint16_t pair = (uint16_t)(((i < 2 ? raw.x : raw.y) >> (16 * (i & 1))) & 0xffffu);
+              const float2 f = __half22float2(e4m3x2_to_half2(pair));
+              const __half2 o = __floats2half2_rn(f.x * sc, f.y * sc);
+              w[i] = *reinterpret_cast<const uint32_t*>(&o);
+            }
+            *reinterpret_cast<uint4*>(stp + b * 512 + r * 32 + ((hh ^ ((r >> 2) & 1)) << 4)) =
+                make_uint4(w[0], w[1], w[2], w[3]);
+          }
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&conv[s]));
+        }
+      }
+    }
+  } else if (warp >= 8) {
     // ---------------------------------------------------------------- copies
     // Stage number c (counted over the CTA's whole run) needs 1 + ntiles
     // bulk copies: copy 0 = the A blocks and the MMA list, copy j = B tile
@@ -195,7 +255,9 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
     uint32_t last_mine = 0xffffffffu;  // last stage this warp copied into (for the drain)
     for (int it = it0; it < it1 && ok; ++it) {
       const WorkItem wi = args.items[args.cta_items[it]];
-      const int stage0 = args.panels[wi.panel].stage_off;
+      const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+      const int n_tiles = P.n_tiles;
+      const int stage0 = P.panels[wi.panel].stage_off;
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
         const int64_t bcol = (int64_t)nt * NSUB;  // first 128-column packed tile of this pass
         for (int base = wi.s0; base < wi.s1 && ok; base += 32) {
@@ -206,24 +268,30 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
           int64_t off1 = 0, off2 = 0, pf_off = 0;
           int bytes1 = 0, total = 0, hword = 0, has2 = 0, pf_bytes = 0;
           if (lane < cnt) {
-            const StageRec* rp = args.stages + stage0 + base + lane;
+            const StageRec* rp = P.stages + stage0 + base + lane;
             const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
             const int4 r1 = reinterpret_cast<const int4*>(rp)[1];           // nblk, hdr_bytes, ntiles, -
             const int ntl = r1.z;
             // this stage's A region, for the L2 prefetch
-            pf_off = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
-            pf_bytes = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
+            if (C::FP8) {
+              pf_off = r0.x * 256 + r1.w + r0.y;
+              pf_bytes = r1.x * 256 + fp8_scale_bytes(r1.x) + r1.y;
+            } else {
+              pf_off = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
+              pf_bytes = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
+            }
             if (j0 == 0) {
-              hword = r1.x * (int)(C::ABLK * C::NOPS);
+              // header position inside the stage
+              hword = C::FP8 ? (int)C::OFF_STG + r1.x * 256 + fp8_scale_bytes(r1.x) : r1.x * (int)(C::ABLK * C::NOPS);
               off1 = pf_off;
               bytes1 = pf_bytes;
               total = bytes1 + ntl * (int)C::TILEB;
               if (ntl == kStageTiles) {
                 has2 = 1;
-                off2 = ((int64_t)rp->kb[kStageTiles - 1] * args.bp_ntiles + bcol) * (4096 * C::NOPS);
+                off2 = ((int64_t)rp->kb[kStageTiles - 1] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
               }
             } else if (j0 <= ntl) {
-              off1 = ((int64_t)rp->kb[j0 - 1] * args.bp_ntiles + bcol) * (4096 * C::NOPS);
+              off1 = ((int64_t)rp->kb[j0 - 1] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
               bytes1 = (int)C::TILEB;
             }
           }
@@ -233,13 +301,13 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
           if (pw < cnt && pw < kPrefetchAhead) {
             const int64_t po = shfl_l(pf_off, pw);
             const int pb = shfl_i(pf_bytes, pw);
-            if (lane == 0) bulk_prefetch_l2(args.aval + po, (uint32_t)pb);
+            if (lane == 0) bulk_prefetch_l2(P.aval + po, (uint32_t)pb);
           }
           for (int i = 0; i < cnt; ++i, ++ci) {
             if (i + kPrefetchAhead < cnt) {
               const int64_t po = shfl_l(pf_off, i + kPrefetchAhead);
               const int pb = shfl_i(pf_bytes, i + kPrefetchAhead);
-              if (lane == 0 && (int)(((uint32_t)pw - ci) & 7u) == 0) bulk_prefetch_l2(args.aval + po, (uint32_t)pb);
+              if (lane == 0 && (int)(((uint32_t)pw - ci) & 7u) == 0) bulk_prefetch_l2(P.aval + po, (uint32_t)pb);
             }
             const int b1 = shfl_i(bytes1, i);
             const int h2 = shfl_i(has2, i);
@@ -263,12 +331,12 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
                 } else if (j == 0) {
                   *reinterpret_cast<uint32_t*>(smem + s * C::STAGE + C::OFF_HW) = (uint32_t)hw;
                   mbar_arrive_expect_tx(fb, (uint32_t)tot);
-                  bulk_load_hint(st, args.aval + o1, (uint32_t)b1, fb, pol_a);
+                  bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), P.aval + o1, (uint32_t)b1, fb, pol_a);
                   if (h2)
-                    bulk_load_hint(st + C::OFF_B + (kStageTiles - 1) * C::TILEB, args.bpack + o2, C::TILEB, fb,
+                    bulk_load_hint(st + C::OFF_B + (kStageTiles - 1) * C::TILEB, P.bpack + o2, C::TILEB, fb,
                                    pol_b);
                 } else {
-                  bulk_load_hint(st + C::OFF_B + (j - 1) * C::TILEB, args.bpack + o1, C::TILEB, fb, pol_b);
+                  bulk_load_hint(st + C::OFF_B + (j - 1) * C::TILEB, P.bpack + o1, C::TILEB, fb, pol_b);
                 }
                 if (b1 != 0) last_mine = ci;
               } else {
@@ -298,11 +366,13 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
       // from the list the copy brought in with the stage, and releases every
       // stage once. One thread issues a tcgen05.mma only every ~80-150
       // cycles; four keep the tensor pipe near its rate for these narrow MMAs.
-      const uint32_t idesc0 = args.idesc;  // without the N field
       uint32_t ci = 0, k = 0;
       bool ok = true, issued = false;
       for (int it = it0; it < it1 && ok; ++it) {
         const WorkItem wi = args.items[args.cta_items[it]];
+        const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+        const int n_tiles = P.n_tiles;
+        const uint32_t idesc0 = P.idesc;  // without the N field
         const int nstages = wi.s1 - wi.s0;
         for (int nt = 0; nt < n_tiles && ok; ++nt, ++k) {
           const uint32_t buf = k & 1;
@@ -318,7 +388,7 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
             const uint32_t s = ci % C::NS;
             // the stage's copies landed (complete_tx); the MMA reads shared
             // memory through the async proxy, so no tcgen05 fence is needed
-            if (!wait_phase(smem_u32(&full[s]), (ci / C::NS) & 1, abort_flag, err, ERR_MMA_A)) {
+            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &full[s]), (ci / C::NS) & 1, abort_flag, err, ERR_MMA_A)) {
               ok = false;
               break;
             }
@@ -383,9 +453,11 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
     bool ok = true;
     for (int it = it0; it < it1 && ok; ++it) {
       const WorkItem wi = args.items[args.cta_items[it]];
+      const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+      const int n_tiles = P.n_tiles;
       const int panel = wi.panel;
       const bool split = wi.split >= 0;
-      const uint32_t slot_mask = args.panels[panel].slot_mask;
+      const uint32_t slot_mask = P.panels[panel].slot_mask;
       for (int nt = 0; nt < n_tiles; ++nt, ++k) {
         const uint32_t buf = k & 1;
         if (!wait_phase(smem_u32(&accfull[buf]), (k >> 1) & 1, abort_flag, err, ERR_EPI)) {
@@ -395,12 +467,12 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
         tc_fence_after();
         const uint32_t dbase = lane_base + buf * C::ACC_COLS;
         // slab of (part, column tile): (first slab of the panel + part) * n_tiles + nt
-        float* slab = split ? args.slabs + ((size_t)(wi.slab + wi.part) * n_tiles + nt) * SLAB : nullptr;
+        float* slab = split ? P.slabs + ((size_t)(wi.slab + wi.part) * n_tiles + nt) * SLAB : nullptr;
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
-          if (rb >= args.nbr) break;
+          if (rb >= P.nbr) break;
           const bool empty_slot = ((slot_mask >> s) & 1u) == 0;
-          const int myrow = (!split && lane < BH) ? args.row_map[(int64_t)rb * BH + lane] : -1;
+          const int myrow = (!split && lane < BH) ? P.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
             const int nl = j * 128 + (int)q * 32 + lane;  // column inside the tile
@@ -423,12 +495,12 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
 #pragma unroll
                 for (int m = 0; m < 16; ++m) {
                   const int row = __shfl_sync(0xffffffffu, myrow, h + m);
-                  if (row >= 0 && n < args.N) {
-                    const int64_t off = (int64_t)row * args.ldc + n;
-                    if (args.c_f16)
-                      __stcs(reinterpret_cast<__half*>(args.C) + off, __float2half_rn(v[m]));
+                  if (row >= 0 && n < P.N) {
+                    const int64_t off = (int64_t)row * P.ldc + n;
+                    if (P.c_f16)
+                      __stcs(reinterpret_cast<__half*>(P.C) + off, __float2half_rn(v[m]));
                     else
-                      __stcs(reinterpret_cast<float*>(args.C) + off, v[m]);
+                      __stcs(reinterpret_cast<float*>(P.C) + off, v[m]);
                   }
                 }
               }
@@ -446,17 +518,17 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
         __syncwarp();
         int last = 0;
         if (lane == 0) {
-          int* ctr = args.counters + ((size_t)wi.split * n_tiles + nt) * 4 + q;
+          int* ctr = P.counters + ((size_t)wi.split * n_tiles + nt) * 4 + q;
           last = atomicAdd(ctr, 1) == wi.nparts - 1;
         }
         last = __shfl_sync(0xffffffffu, last, 0);
         if (!last) continue;
         __threadfence();
-        const float* slab0 = args.slabs + ((size_t)wi.slab * n_tiles + nt) * SLAB;
+        const float* slab0 = P.slabs + ((size_t)wi.slab * n_tiles + nt) * SLAB;
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
-          if (rb >= args.nbr) break;
-          const int myrow = lane < BH ? args.row_map[(int64_t)rb * BH + lane] : -1;
+          if (rb >= P.nbr) break;
+          const int myrow = lane < BH ? P.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
             const int nl = j * 128 + (int)q * 32 + lane;
@@ -479,12 +551,12 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
 #pragma unroll
               for (int m = 0; m < 16; ++m) {
                 const int row = __shfl_sync(0xffffffffu, myrow, h + m);
-                if (row >= 0 && n < args.N) {
-                  const int64_t off = (int64_t)row * args.ldc + n;
-                  if (args.c_f16)
-                    __stcs(reinterpret_cast<__half*>(args.C) + off, __float2half_rn(acc[m]));
+                if (row >= 0 && n < P.N) {
+                  const int64_t off = (int64_t)row * P.ldc + n;
+                  if (P.c_f16)
+                    __stcs(reinterpret_cast<__half*>(P.C) + off, __float2half_rn(acc[m]));
                   else
-                    __stcs(reinterpret_cast<float*>(args.C) + off, acc[m]);
+                    __stcs(reinterpret_cast<float*>(P.C) + off, acc[m]);
                 }
               }
             }
@@ -502,15 +574,32 @@ __global__ void __launch_bounds__(512, 1) spmm_tc_kernel(const __grid_constant__
   }
 }
 
+// Raises the variant's dynamic shared memory limit once per device (a
+// launch inside a stream capture then makes no other CUDA call).
 template <int BH, int R, int NSUB, int KIND>
-static cudaError_t launch_one(const SpmmArgs& args, int grid, cudaStream_t stream) {
+static cudaError_t prepare_one() {
   using C = Cfg<BH, R, NSUB, KIND>;
-  auto kfn = spmm_tc_kernel<BH, R, NSUB, KIND>;
-  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+  static std::atomic<uint64_t> done{0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
+  if (bit && (done.load() & bit)) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(spmm_tc_kernel<BH, R, NSUB, KIND>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
   if (e != cudaSuccess) {
     cudaGetLastError();  // do not leave the error for the next call to find
     return e;
   }
+  done.fetch_or(bit);
+  return cudaSuccess;
+}
+
+template <int BH, int R, int NSUB, int KIND>
+static cudaError_t launch_one(const SpmmArgs& args, int grid, cudaStream_t stream) {
+  using C = Cfg<BH, R, NSUB, KIND>;
+  auto kfn = spmm_tc_kernel<BH, R, NSUB, KIND>;
+  cudaError_t e = prepare_one<BH, R, NSUB, KIND>();
+  if (e != cudaSuccess) return e;
   kfn<<<grid, C::THREADS, C::SMEM_BYTES, stream>>>(args);
   return cudaGetLastError();
 }
@@ -523,7 +612,7 @@ static int ctas_per_sm_one() {
   auto kfn = spmm_tc_kernel<BH, R, NSUB, KIND>;
   int by_tmem = 512 / C::TMEM_COLS;
   int occ = 1;
-  if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES) != cudaSuccess ||
+  if (prepare_one<BH, R, NSUB, KIND>() != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, C::THREADS, C::SMEM_BYTES) != cudaSuccess) {
     cudaGetLastError();
     occ = 1;
@@ -547,28 +636,31 @@ static int ctas_per_sm_one() {
   X(16, 8, 1, 1)            \
   X(16, 16, 1, 1)           \
   X(32, 4, 1, 1)            \
-  X(32, 8, 1, 1)
+  X(32, 8, 1, 1)            \
+  X(16, 4, 1, 2)            \
+  X(16, 8, 1, 2)            \
+  X(16, 16, 1, 2)
 
-bool tc_variant_supported(int bh, int R, int nsub, bool split) {
+bool tc_variant_supported(int bh, int R, int nsub, int kind) {
 #define SMAT_TC_MATCH(BH, R_, NS, K) \
-  if (bh == BH && R == R_ && nsub == NS && (split ? 1 : 0) == K) return true;
+  if (bh == BH && R == R_ && nsub == NS && kind == K) return true;
   SMAT_TC_VARIANTS(SMAT_TC_MATCH)
 #undef SMAT_TC_MATCH
   return false;
 }
 
-int tc_ctas_per_sm(int bh, int R, int nsub, bool split) {
+int tc_ctas_per_sm(int bh, int R, int nsub, int kind) {
 #define SMAT_TC_OCC(BH, R_, NS, K) \
-  if (bh == BH && R == R_ && nsub == NS && (split ? 1 : 0) == K) return dev::ctas_per_sm_one<BH, R_, NS, K>();
+  if (bh == BH && R == R_ && nsub == NS && kind == K) return dev::ctas_per_sm_one<BH, R_, NS, K>();
   SMAT_TC_VARIANTS(SMAT_TC_OCC)
 #undef SMAT_TC_OCC
   return 1;
 }
 
-cudaError_t tc_launch(int bh, int R, int nsub, bool split, const SpmmArgs& args, int grid,
+cudaError_t tc_launch(int bh, int R, int nsub, int kind, const SpmmArgs& args, int grid,
                       cudaStream_t stream) {
 #define SMAT_TC_LAUNCH(BH, R_, NS, K)                             \
-  if (bh == BH && R == R_ && nsub == NS && (split ? 1 : 0) == K) \
+  if (bh == BH && R == R_ && nsub == NS && kind == K) \
     return dev::launch_one<BH, R_, NS, K>(args, grid, stream);
   SMAT_TC_VARIANTS(SMAT_TC_LAUNCH)
 #undef SMAT_TC_LAUNCH

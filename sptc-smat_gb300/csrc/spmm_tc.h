@@ -33,16 +33,23 @@ struct PanelInfo {
 // the split form, else 1) a stage occupies
 //     [nblk * ABLK blocks (hi)][nblk * ABLK blocks (lo, split form only)][header]
 // starting at byte blk_off * ABLK * NOPS + hdr_off, where hdr_off is the sum
-// of the header bytes of all earlier stages.
+// of the header bytes of all earlier stages. In the FP8 stream (16 x 16
+// blocks) a stage occupies
+//     [nblk * 256 e4m3 blocks][nblk FP32 scales, padded to 16 bytes][header]
+// starting at byte blk_off * 256 + scl_off + hdr_off, where scl_off is the
+// sum of the padded scale bytes of all earlier stages.
 struct StageRec {
   int64_t blk_off;     // blocks before this stage (stream order)
   int64_t hdr_off;     // header bytes before this stage
   int32_t nblk;        // A blocks in the stage
   int32_t hdr_bytes;   // bytes of this stage's header (multiple of 16)
   int32_t ntiles;      // B tiles (distinct block columns) of the stage, 1..kStageTiles
-  int32_t pad;
+  int32_t scl_off;     // padded FP8 scale bytes before this stage
   int32_t kb[kStageTiles];  // k-block (column / 16) of each tile
 };
+
+// Padded bytes of the FP32 scales of n FP8 blocks.
+__host__ __device__ constexpr int fp8_scale_bytes(int n) { return (4 * n + 15) / 16 * 16; }
 
 // Stage header (little-endian), kStageHdrFixed bytes then one 32-bit entry
 // per MMA group, grouped by issuing warp:
@@ -72,36 +79,48 @@ struct WorkItem {
   int32_t part;        // part number within the split panel
   int32_t nparts;      // parts of the split panel
   int32_t slab;        // first slab of the split panel (one per part and column tile)
-  int32_t pad;
+  int32_t prob;        // problem of a grouped launch (0 for a single SpMM)
 };
 
-// Kernel arguments (one __grid_constant__ parameter).
-struct SpmmArgs {
+// Everything the kernel needs about one SpMM problem.
+struct ProblemDesc {
   const uint8_t* bpack;      // B in 4 KB tiles [k-block][128-column tile] (pack_b); the split
                              // form stores [hi tile | lo tile] pairs, 8 KB per tile
   int64_t bp_ntiles;         // 128-column tiles per k-block in bpack
   const uint8_t* aval;       // A stream of the form (see StageRec)
   const PanelInfo* panels;
   const StageRec* stages;
-  const int32_t* cta_ptr;    // [grid + 1]
-  const int32_t* cta_items;  // work items, per CTA
-  const WorkItem* items;
-  float* slabs;              // partial sums of split panels: [slab][R * bh rows][BN] FP32
-  int32_t* counters;         // [split panels][column tiles], zero before the launch
   const int32_t* row_map;    // [rows_padded] BCSR row -> C row, or -1
   void* C;
   int64_t ldc;
+  float* slabs;              // partial sums of split panels: [slab][R * bh rows][BN] FP32
+  int32_t* counters;         // [split panels][column tiles][4], zero before the launch
   int32_t N;
   int32_t n_tiles;
   int32_t nbr;
   int32_t c_f16;
-  uint32_t idesc;
+  uint32_t idesc;            // instruction descriptor without the N field
+  int32_t pad[3];
+};
+
+// Kernel arguments (one __grid_constant__ parameter). A single SpMM passes
+// its problem by value (one); a grouped launch passes a device array
+// (probs, indexed by WorkItem::prob).
+struct SpmmArgs {
+  ProblemDesc one;
+  const ProblemDesc* probs;
+  const int32_t* cta_ptr;    // [grid + 1]
+  const int32_t* cta_items;  // work items, per CTA
+  const WorkItem* items;
   int* err;
 };
 
-bool tc_variant_supported(int bh, int R, int nsub, bool split);
-int tc_ctas_per_sm(int bh, int R, int nsub, bool split);
-cudaError_t tc_launch(int bh, int R, int nsub, bool split, const SpmmArgs& args, int grid,
+// Kernel kinds: 0 plain (FP16 or BF16 A and B), 1 split hi+lo BF16, 2 FP8 A
+// (e4m3 + per-block scale, converted to FP16 in shared memory).
+enum : int { TC_KIND_PLAIN = 0, TC_KIND_SPLIT = 1, TC_KIND_FP8 = 2 };
+bool tc_variant_supported(int bh, int R, int nsub, int kind);
+int tc_ctas_per_sm(int bh, int R, int nsub, int kind);
+cudaError_t tc_launch(int bh, int R, int nsub, int kind, const SpmmArgs& args, int grid,
                       cudaStream_t stream);
 
 }  // namespace smat

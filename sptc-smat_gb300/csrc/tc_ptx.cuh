@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 
 namespace smat {
@@ -110,6 +111,19 @@ __device__ __forceinline__ uint64_t make_l2_policy_evict_last() {
 }
 __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* tm) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm)) : "memory");
+}
+
+// Generic-proxy writes to shared memory made visible to the async proxy
+// (the tensor core's operand reads) before a barrier hands them over.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Two e4m3 values (low byte -> low half) to two FP16 values, exactly.
+__device__ __forceinline__ __half2 e4m3x2_to_half2(uint16_t v) {
+  uint32_t r;
+  asm("cvt.rn.f16x2.e4m3x2 %0, %1;" : "=r"(r) : "h"(v));
+  return *reinterpret_cast<__half2*>(&r);
 }
 
 // ---------------------------------------------------------------- tcgen05

@@ -22,9 +22,10 @@ from dataclasses import dataclass
 import numpy as np
 
 from ._lib import (BF16, COL_MAJOR, E4M3, F16, F32, F64, FORM_BF16, FORM_F16, FORM_FP8, FORM_SPLIT_BF16,
-                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrFile, CsrStruct, ReorderStats, SmatError, check, lib, ptr)
+                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrFile, CsrStruct, Problem, ReorderStats, SmatError, TuneResult,
+                   check, lib, ptr)
 
-__all__ = ["Csr", "Bcsr", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
+__all__ = ["Csr", "Bcsr", "Group", "autotune", "features", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
            "FORM_FP8", "FORM_SPLIT_BF16", "F32", "F16", "BF16", "F64", "E4M3", "ROW_MAJOR", "COL_MAJOR"]
 
 _VAL_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float16): F16, np.dtype(np.float64): F64}
@@ -165,6 +166,11 @@ def csr_to_bcsr_host(csr: Csr, block=(16, 16), row_perm=None):
     return rp, ci[:n], vals[: n * bh * bw].view(np.float16).reshape(n, bh, bw)
 
 
+def _torch_dt(dt):
+    import torch
+    return {torch.float32: F32, torch.float16: F16, torch.bfloat16: BF16}[dt]
+
+
 def _torch_layout(t):
     """(layout, ld) of a 2-D torch tensor viewed as (K, N)."""
     if t.dim() != 2:
@@ -296,6 +302,72 @@ class Bcsr:
 
     def check_device_error(self):
         check(lib().smat_bcsr_check_device_error(self._h))
+
+
+def autotune(csr: Csr, form: int = FORM_F16, N: int = 128, block=(16, 16), row_perm=None, device: int = 0) -> dict:
+    """Measure the launch shapes for this matrix and cache the fastest (smat_autotune)."""
+    o = BcsrOpts()
+    o.block_rows, o.block_cols = block
+    perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
+    o.row_perm = None if perm is None else perm.ctypes.data
+    o.device = device
+    r = TuneResult()
+    s = csr.struct()
+    check(lib().smat_autotune(C.byref(s), C.byref(o), form, N, C.byref(r)))
+    return {"panel_rows": r.panel_rows, "split_frac": r.split_frac, "ms": r.ms, "ms_default": r.ms_default,
+            "cached": bool(r.cached)}
+
+
+def features(csr: Csr, device: int = 0) -> np.ndarray:
+    """The 64 matrix features of smat_features (computed on the GPU)."""
+    out = np.zeros(64, np.float32)
+    s = csr.struct()
+    check(lib().smat_features(C.byref(s), device, out.ctypes.data))
+    return out
+
+
+class Group:
+    """Many SpMMs in one persistent launch (smat_group_*). problems: list of
+    (Bcsr, form, B, C) with torch CUDA tensors; B is (K, N) in either layout,
+    C is (rows, N) row-major FP32 or FP16. The tensors must stay alive and in
+    place while the group is used."""
+
+    def __init__(self, problems):
+        arr = (Problem * len(problems))()
+        self._keep = []
+        for i, (M, form, B, Cm) in enumerate(problems):
+            layout, ld = _torch_layout(B)
+            arr[i].A = M.handle.value if hasattr(M.handle, "value") else M.handle
+            arr[i].form = form
+            arr[i].B = B.data_ptr()
+            arr[i].b_dtype = _torch_dt(B.dtype)
+            arr[i].b_layout = layout
+            arr[i].ldb = ld
+            arr[i].C = Cm.data_ptr()
+            arr[i].c_dtype = _torch_dt(Cm.dtype)
+            arr[i].ldc = Cm.stride(0)
+            arr[i].N = B.shape[1]
+            self._keep.append((M, B, Cm))
+        h = C.c_void_p()
+        check(lib().smat_group_create(arr, len(problems), C.byref(h)))
+        self._h = h
+
+    def run(self, stream=0):
+        check(lib().smat_group_run(self._h, stream))
+
+    def check_device_error(self):
+        check(lib().smat_group_check_device_error(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().smat_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def partition_rows(csr: Csr, world: int, block_rows: int = 16):

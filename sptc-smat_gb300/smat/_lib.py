@@ -39,6 +39,17 @@ class CsrFile(C.Structure):
     _fields_ = [("csr", CsrStruct), ("symmetric", C.c_int32)]
 
 
+class Problem(C.Structure):
+    _fields_ = [("A", C.c_void_p), ("form", C.c_int32), ("B", C.c_void_p), ("b_dtype", C.c_int32),
+                ("b_layout", C.c_int32), ("ldb", C.c_int64), ("C", C.c_void_p), ("c_dtype", C.c_int32),
+                ("ldc", C.c_int64), ("N", C.c_int64)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("panel_rows", C.c_int32), ("split_frac", C.c_float), ("ms", C.c_double),
+                ("ms_default", C.c_double), ("cached", C.c_int32)]
+
+
 class BcsrInfo(C.Structure):
     _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("rows_padded", C.c_int64),
                 ("cols_padded", C.c_int64), ("nnz", C.c_int64), ("nnzb", C.c_int64),
@@ -63,6 +74,7 @@ _SIGS = {
     "smat_bcsr_create_from_bcsr": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.POINTER(BcsrOpts), C.POINTER(C.c_void_p)]),
     "smat_bcsr_destroy": (C.c_int, [C.c_void_p]),
+    "smat_bcsr_export_fp8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "smat_bcsr_get_info": (C.c_int, [C.c_void_p, C.POINTER(BcsrInfo)]),
     "smat_bcsr_export": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "smat_csr_to_bcsr_host": (C.c_int, [C.POINTER(CsrStruct), C.c_int32, C.c_int32, C.c_void_p,
@@ -76,6 +88,24 @@ _SIGS = {
                                    C.c_void_p]),
     "smat_spmm_static_scratch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64,
                                            C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
+    "smat_autotune": (C.c_int, [C.POINTER(CsrStruct), C.POINTER(BcsrOpts), C.c_int32, C.c_int64,
+                                C.POINTER(TuneResult)]),
+    "smat_autotune_clear": (C.c_int, []),
+    "smat_features": (C.c_int, [C.POINTER(CsrStruct), C.c_int32, C.c_void_p]),
+    "smat_mlp_create": (C.c_int, [C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "smat_mlp_num_params": (C.c_int32, []),
+    "smat_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smat_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smat_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                     C.c_void_p]),
+    "smat_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float,
+                                      C.c_void_p]),
+    "smat_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "smat_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "smat_group_create": (C.c_int, [C.POINTER(Problem), C.c_int32, C.POINTER(C.c_void_p)]),
+    "smat_group_run": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smat_group_check_device_error": (C.c_int, [C.c_void_p]),
+    "smat_group_destroy": (C.c_int, [C.c_void_p]),
     "smat_spmm_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                                  C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
     "smat_bcsr_check_device_error": (C.c_int, [C.c_void_p]),

@@ -1,0 +1,65 @@
+"""GPU: the learned tau / block-shape predictor's kernels (csrc/mlp.cu).
+Gradients of one batch against the FP64 numpy oracle (oracle/mlp_oracle.py,
+relative 1e-4 on every parameter block), predictions against the oracle's
+forward pass, and Adam reducing the loss on a fixed batch."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def net(smat_mod):
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    L = smat_mod.lib()
+    h = C.c_void_p()
+    assert L.smat_mlp_create(0, 1234, C.byref(h)) == 0, L.smat_last_error()
+    yield L, h
+    L.smat_mlp_destroy(h)
+
+
+def batch(B, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(0, 1, (B, 64)).astype(np.float32)
+    return X, rng.integers(0, 9, B).astype(np.int32), rng.integers(1, 3, B).astype(np.int32)
+
+
+def test_gradients_match_fp64_oracle(net):
+    import mlp_oracle
+    L, h = net
+    n = L.smat_mlp_num_params()
+    p = np.zeros(n, np.float32)
+    assert L.smat_mlp_get_params(h, p.ctypes.data) == 0
+    X, yt, yb = batch(96, 1)
+    g = np.zeros(n, np.float32)
+    loss = np.zeros(1, np.float32)
+    assert L.smat_mlp_gradients(h, X.ctypes.data, yt.ctypes.data, yb.ctypes.data, 96, g.ctypes.data,
+                                loss.ctypes.data) == 0
+    ref_loss, ref_g, ref_logits = mlp_oracle.loss_and_grad(p, X, yt, yb)
+    assert abs(loss[0] - ref_loss) <= 1e-5 * max(1.0, abs(ref_loss))
+    o = 0
+    for name, shape in mlp_oracle.SIZES:
+        k = int(np.prod(shape))
+        a, b = g[o:o + k].astype(np.float64), ref_g[o:o + k]
+        assert np.linalg.norm(a - b) <= 1e-4 * max(np.linalg.norm(b), 1e-12), name
+        o += k
+    logits = np.zeros((96, 12), np.float32)
+    assert L.smat_mlp_predict(h, X.ctypes.data, 96, logits.ctypes.data) == 0
+    assert np.allclose(logits, ref_logits, rtol=1e-4, atol=1e-5)
+
+
+def test_adam_reduces_loss(net):
+    L, h = net
+    X, yt, yb = batch(128, 2)
+    loss = np.zeros(1, np.float32)
+    first = None
+    for step in range(200):
+        assert L.smat_mlp_train_step(h, X.ctypes.data, yt.ctypes.data, yb.ctypes.data, 128, C.c_float(3e-3),
+                                     loss.ctypes.data) == 0
+        if first is None:
+            first = float(loss[0])
+    assert float(loss[0]) < 0.25 * first, (first, float(loss[0]))

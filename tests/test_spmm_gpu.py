@@ -217,3 +217,68 @@ def test_reference_kernel_agrees(dev, smat_mod, oracle_lib):
     e_pair = rel_err(ours, Cref.float().cpu().numpy().astype(np.float64))
     assert e_ours <= 1e-3 and e_ours <= e_ref
     assert e_pair <= 1e-3, (e_pair, e_ref, e_ours)
+
+
+def e4m3_table():
+    """Value of every e4m3 ("e4m3fn": bias 7, no infinities, 0x7f/0xff NaN) code."""
+    t = np.zeros(256, np.float64)
+    for c in range(256):
+        s = -1.0 if c & 0x80 else 1.0
+        e, m = (c >> 3) & 0xF, c & 7
+        if e == 0xF and m == 7:
+            t[c] = np.nan
+        elif e == 0:
+            t[c] = s * m * 2.0 ** -9
+        else:
+            t[c] = s * (1 + m / 8) * 2.0 ** (e - 7)
+    return t
+
+
+def test_fp8_form_exact_and_within_budget(dev, smat_mod, oracle_lib):
+    """FP8 form: e4m3 A with one FP32 scale per 16x16 block. The kernel must
+    reproduce the FP64 product of its own dequantised A (FP32 accumulation,
+    1e-5), and that A must stay within the 2e-2 budget of the FP64 product of
+    the FP32 matrix (27-point stencil, FP32 B)."""
+    import ctypes as C
+    from smat import generators as G
+    A = G.stencil27(16)
+    Bf = np.random.default_rng(12).standard_normal((A.cols, 96)).astype(np.float32)
+    M = smat_mod.Bcsr(A, forms=(smat_mod.FORM_FP8, smat_mod.FORM_F16))
+    got = spmm(M, torch.from_numpy(Bf).to(dev), smat_mod.FORM_FP8)
+    nnzb = M.info["nnzb"]
+    codes = np.zeros(nnzb * 256, np.uint8)
+    scales = np.zeros(nnzb, np.float32)
+    assert smat_mod.lib().smat_bcsr_export_fp8(M.handle, codes.ctypes.data, scales.ctypes.data) == 0
+    rp, ci, _, _ = M.export()
+    deq = (e4m3_table()[codes].reshape(nnzb, 16, 16) * scales[:, None, None].astype(np.float64))
+    deq = deq.astype(np.float32).astype(np.float16).astype(np.float64)     # the FP16 operand the MMA reads
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    Cq = np.zeros((M.info["rows_padded"], 96))
+    for b in range(nnzb):
+        r0, c0 = rows[b] * 16, ci[b]
+        Cq[r0:r0 + 16] += deq[b] @ Bf[c0:c0 + 16].astype(np.float16).astype(np.float64)   # B is packed to FP16
+    assert rel_err(got, Cq[: A.rows]) <= 1e-5
+    e8 = rel_err(got, fp64_product(oracle_lib, A, Bf))
+    assert e8 <= 2e-2, e8
+    # plain max-abs scaling (block max -> 448) for comparison: the chosen scales do better
+    vals = np.zeros((nnzb, 16, 16))
+    Asp = A.to_scipy().tocoo()
+    bi = {(int(r), int(c)): k for k, (r, c) in enumerate(zip(rows, ci))}
+    for r, c, v in zip(Asp.row, Asp.col, Asp.data):
+        vals[bi[(r // 16, c // 16 * 16)], r % 16, c % 16] = v
+    amax = np.abs(vals).reshape(nnzb, -1).max(1)
+    tab = e4m3_table()
+    grid = np.sort(np.unique(np.abs(tab[~np.isnan(tab)])))
+    def q(x):
+        a = np.abs(x)
+        idx = np.clip(np.searchsorted(grid, a), 1, len(grid) - 1)
+        lo, hi = grid[idx - 1], grid[idx]
+        return np.sign(x) * np.where(a - lo <= hi - a, lo, hi)
+    plain = q(vals / (amax / 448)[:, None, None]) * (amax / 448)[:, None, None]
+    assert np.sum((deq - vals) ** 2) < np.sum((plain - vals) ** 2)
+
+
+def test_fp8_form_rejects_out_of_range_values(dev, smat_mod):
+    A = smat_mod.Csr(16, 16, np.array([0] * 16 + [1]), np.array([3]), np.array([1e6], np.float32))
+    with pytest.raises(smat_mod.SmatError):
+        smat_mod.Bcsr(A, forms=(smat_mod.FORM_FP8,))
