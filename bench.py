@@ -440,19 +440,107 @@ def run_forms(args):
         del ws
 
 
+BATCH_WORKLOAD = {
+    "workload": "batched512_uneven",
+    "generator": "512 matrices, rows log-uniform in [1024, 32768]; 1/3 band (half-bandwidth 8-256), 1/3 R-MAT "
+                 "(average degree 8-64), 1/3 random 16x16 blocks (1-5 % block density, 40-90 % fill); "
+                 "N in {32, 64, 128}; FP16 or BF16 A and B; FP32 C",
+    "grouped": "smat_group_run (grouped B packing + one persistent SpMM launch) replayed from a CUDA graph",
+    "sequential": "512 smat_spmm calls (pack + SpMM each) on one stream",
+}
+
+
+def run_batched(args):
+    """Many uneven SpMMs: one grouped launch (CUDA graph) against sequential single calls."""
+    import torch
+
+    import smat
+    from smat import generators as G
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(11)
+    count = args.batch_count
+    t0 = time.time()
+    probs = []
+    useful = 0.0
+    for i in range(count):
+        rows = int(np.exp(rng.uniform(np.log(1024), np.log(32768))))
+        fam = i % 3
+        if fam == 0:
+            A = G.band(rows, int(np.exp(rng.uniform(np.log(8), np.log(256)))), seed=i)
+        elif fam == 1:
+            scale = int(np.ceil(np.log2(rows)))
+            A = G.rmat(scale, int(rng.uniform(8, 64) * (1 << scale)), seed=i)
+        else:
+            A = G.random_block(rows, float(rng.uniform(0.01, 0.05)), 0.4, 0.9, seed=i)
+        N = int(rng.choice([32, 64, 128]))
+        form = smat.FORM_F16 if i % 2 == 0 else smat.FORM_BF16
+        tdt = torch.float16 if form == smat.FORM_F16 else torch.bfloat16
+        M = smat.Bcsr(A, forms=(form,))
+        B = torch.randn((A.cols, N), device=dev).to(tdt)
+        Cg = torch.empty((A.rows, N), dtype=torch.float32, device=dev)
+        Cs = torch.empty_like(Cg)
+        ws = torch.empty(M.workspace_size(form, smat.F16 if form == smat.FORM_F16 else smat.BF16, N),
+                         dtype=torch.uint8, device=dev)
+        probs.append((M, form, B, Cg, Cs, ws, N))
+        useful += 2.0 * A.nnz * N
+    log(f"[bench] {count} matrices built in {time.time() - t0:.1f}s, useful {useful / 1e9:.2f} GFLOP")
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+
+    def sequential():
+        for M, form, B, Cg, Cs, ws, N in probs:
+            M.spmm(B, form=form, out=Cs, workspace=ws, stream=sp)
+
+    g = smat.Group([(M, form, B, Cg) for M, form, B, Cg, Cs, ws, N in probs])
+    g.run(sp)
+    stream.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        g.run(sp)
+
+    def timed(fn, reps):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+
+    with torch.cuda.stream(stream):
+        ms_seq = timed(sequential, max(2, args.steps // 5))
+        ms_grp = timed(graph.replay, args.steps)
+    g.check_device_error()
+    diff = max(float((Cg - Cs).abs().max() / Cs.abs().max().clamp_min(1e-30)) for M, f, B, Cg, Cs, ws, N in probs)
+    print(json.dumps({"metric": METRIC, "workload": BATCH_WORKLOAD["workload"],
+                      "value": useful / (ms_grp * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms_grp,
+                      "sequential": {"value": useful / (ms_seq * 1e-3) / 1e12, "ms_per_step": ms_seq},
+                      "speedup_vs_sequential": ms_seq / ms_grp, "max_rel_diff_grouped_vs_sequential": diff,
+                      "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "data": "synthetic",
+                      "config": dict(BATCH_WORKLOAD, count=count, useful_gflop=useful / 1e9)}), flush=True)
+    g.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="smat", choices=["smat", "reference"])
-    ap.add_argument("--workload", default="rmat16", choices=["rmat16", "stencil64_forms"],
-                    help="rmat16: the headline SpMM line; stencil64_forms: one line per precision form")
+    ap.add_argument("--workload", default="rmat16", choices=["rmat16", "stencil64_forms", "batched512"],
+                    help="rmat16: the headline SpMM line; stencil64_forms: one line per precision form; "
+                         "batched512: grouped vs sequential SpMMs")
+    ap.add_argument("--batch-count", type=int, default=512)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "stencil64_forms":
         run_forms(args)
+    elif args.workload == "batched512":
+        run_batched(args)
     else:
         run_smat(args)
 

@@ -97,20 +97,15 @@ def random_block(n: int, block_density: float, fill_lo: float, fill_hi: float, b
     rng = np.random.default_rng(seed)
     nb = (n + bs - 1) // bs
     nblk = max(1, int(round(nb * nb * block_density)))
-    flat = rng.choice(nb * nb, size=min(nblk, nb * nb), replace=False)
-    rs, cs = [], []
-    for f in flat:
-        br, bc = divmod(int(f), nb)
-        fill = rng.uniform(fill_lo, fill_hi)
-        m = rng.random((bs, bs)) < fill
-        rr, cc = np.nonzero(m)
-        rr = rr + br * bs
-        cc = cc + bc * bs
-        ok = (rr < n) & (cc < n)
-        rs.append(rr[ok])
-        cs.append(cc[ok])
-    r = np.concatenate(rs).astype(np.int64)
-    c = np.concatenate(cs).astype(np.int64)
+    flat = rng.choice(nb * nb, size=min(nblk, nb * nb), replace=False).astype(np.int64)
+    br, bc = np.divmod(flat, nb)
+    fill = rng.uniform(fill_lo, fill_hi, size=flat.size).astype(np.float32)
+    m = rng.random((flat.size, bs, bs), dtype=np.float32) < fill[:, None, None]
+    k, rr, cc = np.nonzero(m)
+    r = rr.astype(np.int64) + br[k] * bs
+    c = cc.astype(np.int64) + bc[k] * bs
+    ok = (r < n) & (c < n)
+    r, c = r[ok], c[ok]
     v = rng.standard_normal(r.size).astype(dtype)
     return _csr_from_coo(n, n, r, c, v)
 

@@ -181,6 +181,30 @@ class Selector:
             pass
 
 
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def load_default(device=0):
+    """The selector trained on the committed sweep (data/selector_weights.npz)."""
+    return Selector(device=device, params=np.load(os.path.join(DATA, "selector_weights.npz"))["params"])
+
+
+def choose(csr, selector=None, device=0):
+    """(tau, (block rows, block cols)) for csr: the selector's prediction, or,
+    without one, the exhaustive sweep's best (the fallback)."""
+    from . import features
+    if selector is not None:
+        ti, bi = selector.predict(features(csr, device)[None, :])
+        return TAUS[int(ti[0])], BLOCKS[int(bi[0])]
+    perms = sweep_perms([csr])
+    best, arg = np.inf, None
+    for (m, t, b), perm in perms.items():
+        ms = time_spmm(csr, perm, BLOCKS[b], device)
+        if ms < best:
+            best, arg = ms, (TAUS[t], BLOCKS[b])
+    return arg
+
+
 def regret(T, ti, bi):
     best = T.reshape(len(T), -1).min(1)
     return T[np.arange(len(T)), ti, bi] / best - 1.0

@@ -63,3 +63,30 @@ def test_adam_reduces_loss(net):
         if first is None:
             first = float(loss[0])
     assert float(loss[0]) < 0.25 * first, (first, float(loss[0]))
+
+
+def test_trained_selector_beats_the_default_on_held_out(smat_mod):
+    """Train on the committed sweep (160 seeded matrices, tau 0.1..0.9 x block
+    shapes, BF16 SpMM times measured on a GB300) with the library's kernels
+    and evaluate on its 40 held-out matrices: mean regret against the sweep
+    best within 10 %, and lower than the method without the learned part
+    (tau 0.6, 16x16)."""
+    import os
+    from smat import selector as S
+    d = np.load(os.path.join(S.DATA, "selector_sweep.npz"))
+    X, T, ntr = d["X"], d["T"], int(d["train"])
+    yt, yb = S.labels(T)
+    sel = S.Selector(seed=1)
+    hist = sel.train(X[:ntr], yt[:ntr], yb[:ntr], epochs=400)
+    assert hist[-1] < 0.6 * hist[0]
+    ti, bi = sel.predict(X[ntr:])
+    r = S.regret(T[ntr:], ti, bi)
+    r0 = S.regret(T[ntr:], np.full(len(ti), S.DEFAULT[0]), np.full(len(ti), S.DEFAULT[1]))
+    assert r.mean() <= 0.10, r.mean()
+    assert r.mean() < r0.mean(), (r.mean(), r0.mean())
+    sel.close()
+    # the committed weights load and predict available shapes only
+    w = S.load_default()
+    _, b = w.predict(X[ntr:])
+    assert set(b.tolist()) <= {1, 2}
+    w.close()
