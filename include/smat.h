@@ -327,8 +327,11 @@ smat_status smat_group_run(smat_group* g, void* stream);
 smat_status smat_group_check_device_error(smat_group* g);
 smat_status smat_group_destroy(smat_group* g);
 
-/* Host-buffer variant: copies B (host) in, runs smat_spmm, copies C (host)
- * out, and waits for completion. Uses device buffers cached in the handle. */
+/* Host-buffer variant: B and C in host memory; returns when C is written.
+ * When both are page-locked (cudaHostAlloc / cudaMallocHost / registered),
+ * the kernels read B and write C in place over the CPU-GPU link (GB300:
+ * NVLink-C2C); otherwise B is copied in and C out through device buffers
+ * cached in the handle. */
 smat_status smat_spmm_host(const smat_bcsr* A, int32_t form, const void* B_host, int32_t b_dtype,
                            int32_t b_layout, int64_t ldb, void* C_host, int32_t c_dtype,
                            int64_t ldc, int64_t N, void* stream);

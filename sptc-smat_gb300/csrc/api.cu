@@ -566,9 +566,25 @@ smat_status smat_spmm_host(const smat_bcsr* A_, int32_t form, const void* B_host
     if (e == cudaSuccess) *cap = need;
     return e;
   };
+  SMAT_CUDA(grow(&A->d_ws, &A->ws_bytes, wbytes));
+  // On GB300 the GPU reaches page-locked host memory directly over
+  // NVLink-C2C: when both buffers are pinned, B is read and C written in
+  // place by the pack and SpMM kernels, and no staging copies are made.
+  cudaPointerAttributes pa{}, pc{};
+  const bool b_pinned = cudaPointerGetAttributes(&pa, B_host) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                        pa.devicePointer != nullptr;
+  const bool c_pinned = cudaPointerGetAttributes(&pc, C_host) == cudaSuccess && pc.type == cudaMemoryTypeHost &&
+                        pc.devicePointer != nullptr;
+  cudaGetLastError();
+  if (b_pinned && c_pinned) {
+    smat_status s = smat_spmm(A, form, pa.devicePointer, b_dtype, b_layout, ldb, pc.devicePointer, c_dtype, ldc, N,
+                              A->d_ws, A->ws_bytes, stream);
+    if (s != SMAT_OK) return s;
+    SMAT_CUDA(cudaStreamSynchronize(stream));
+    return SMAT_OK;
+  }
   SMAT_CUDA(grow(&A->d_bstage, &A->bstage_bytes, bbytes));
   SMAT_CUDA(grow(&A->d_cstage, &A->cstage_bytes, std::max<size_t>(cbytes, 1)));
-  SMAT_CUDA(grow(&A->d_ws, &A->ws_bytes, wbytes));
   SMAT_CUDA(cudaMemcpyAsync(A->d_bstage, B_host, bbytes, cudaMemcpyHostToDevice, stream));
   smat_status s = smat_spmm(A, form, A->d_bstage, b_dtype, b_layout, ldb, A->d_cstage, c_dtype, ldc,
                             N, A->d_ws, A->ws_bytes, stream);

@@ -143,12 +143,31 @@ __global__ void pack_b_grouped_kernel(const PackJob* __restrict__ jobs, int njob
   }
 }
 
+// Column-major B with 16-byte aligned columns: warp w of a block packs
+// column n = blockIdx.y * 8 + w for 32 consecutive k-blocks (lane = k-block),
+// so a warp reads 32 consecutive 32-byte pieces of one column (1 KB,
+// contiguous) -- the access shape that also suits B in host memory read over
+// the CPU-GPU link -- and each lane writes its 32-byte row of one tile.
+template <typename T, int OUT>
+__global__ void pack_b_colmajor(const T* __restrict__ in, int64_t ldi, uint8_t* __restrict__ out, int64_t K,
+                                int64_t N, int ntiles, int64_t kbs) {
+  const int64_t kb = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+  const int64_t n = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (kb >= kbs || n >= (int64_t)ntiles * 128) return;
+  pack_tile<T, OUT>(in, 1, ldi, out, K, N, ntiles, kb, (int)(n >> 7), (int)(n & 127));
+}
+
 template <typename T, int OUT>
 static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* out, int64_t K, int64_t N,
                             cudaStream_t s) {
   const int ntiles = (int)packed_b_tiles(N);
   const int64_t kbs = (K + 15) / 16;
   if (kbs == 0 || ntiles == 0) return cudaSuccess;
+  if (layout == 1 && ((reinterpret_cast<uintptr_t>(in) | (uint64_t)ldi * sizeof(T)) & 15) == 0) {
+    dim3 grid((unsigned)((kbs + 31) / 32), (unsigned)((int64_t)ntiles * 128 / 8));
+    pack_b_colmajor<T, OUT><<<grid, 256, 0, s>>>((const T*)in, ldi, out, K, N, ntiles, kbs);
+    return cudaGetLastError();
+  }
   dim3 grid((unsigned)ntiles, (unsigned)kbs);
   pack_b_tiles<T, OUT><<<grid, 128, 0, s>>>((const T*)in, layout, ldi, out, K, N, ntiles);
   return cudaGetLastError();

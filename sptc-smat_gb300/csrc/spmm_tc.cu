@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       // from the list the copy brought in with the stage, and releases every
       // stage once. One thread issues a tcgen05.mma only every ~80-150
       // cycles; four keep the tensor pipe near its rate for these narrow MMAs.
-      uint32_t ci = 0, k = 0;
+      uint32_t ci = 0, k = 0, slot_s = 0, phase_s = 0;
       bool ok = true, issued = false;
       for (int it = it0; it < it1 && ok; ++it) {
         const WorkItem wi = args.items[args.cta_items[it]];
@@ -385,10 +385,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
           }
           tc_fence_after();
           for (int c = 0; c < nstages; ++c, ++ci) {
-            const uint32_t s = ci % C::NS;
+            const uint32_t s = slot_s;  // == ci % NS, kept incrementally
             // the stage's copies landed (complete_tx); the MMA reads shared
             // memory through the async proxy, so no tcgen05 fence is needed
-            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &full[s]), (ci / C::NS) & 1, abort_flag, err, ERR_MMA_A)) {
+            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &full[s]), phase_s, abort_flag, err, ERR_MMA_A)) {
               ok = false;
               break;
             }
@@ -421,6 +421,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               issued = true;
             }
             umma_commit(smem_u32(&empty[s]));
+            if (++slot_s == (uint32_t)C::NS) {
+              slot_s = 0;
+              phase_s ^= 1u;
+            }
           }
           if (!ok) break;
           umma_commit(smem_u32(&accfull[buf]));

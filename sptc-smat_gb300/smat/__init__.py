@@ -280,7 +280,8 @@ class Bcsr:
     def spmm_host(self, B: np.ndarray, form: int = FORM_F16, out_dtype=np.float32, out=None,
                   stream=0) -> np.ndarray:
         """Host-buffer SpMM (smat_spmm_host): B (K, N) numpy in, C (rows, N) numpy out.
-        Pinned host buffers make the copies asynchronous DMA."""
+        With page-locked B and C (e.g. views of torch pin_memory tensors) the
+        kernels read B and write C in place over the CPU-GPU link."""
         B = np.asarray(B)
         K, N = B.shape
         b_dtype = {np.dtype(np.float32): F32, np.dtype(np.float16): F16}[B.dtype]
