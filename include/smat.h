@@ -189,6 +189,20 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
                                   const int64_t* row_perm, int64_t* nnzb, int32_t* row_ptr,
                                   int32_t* col_idx, uint16_t* values_f16);
 
+/* The reference's 2:4 / dense split of the blocks (filterBcsrBlocks,
+ * matrix.h:1140-1288, with the blockInfo labels of csrToBcsr :679-711),
+ * host only, bit-identical: blocks the reference labels 1 ("2:4": no row of
+ * the block holds three consecutive columns in file order ending at a
+ * column % 4 of 2 or 3) go to the first BCSR, the others (2, dense) to the
+ * second, each in block-row and column order; block_info (optional) gets
+ * the label grid [rows_padded/16][cols_padded/block_cols] (0 = empty).
+ * 16-row blocks, block_cols 16 or 32. Call with row_ptr_24 == NULL for the
+ * counts. */
+smat_status smat_csr_to_bcsr_split_host(const smat_csr* A, int32_t block_cols, const int64_t* row_perm,
+                                        int64_t* n_24, int64_t* n_dense, int32_t* row_ptr_24, int32_t* col_idx_24,
+                                        uint16_t* values_24, int32_t* row_ptr_dense, int32_t* col_idx_dense,
+                                        uint16_t* values_dense, int32_t* block_info);
+
 /* ---------------------------------------------------------------- step 3 */
 
 /* Bytes of device scratch smat_spmm needs for this form / B dtype / N: the

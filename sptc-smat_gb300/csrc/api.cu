@@ -453,6 +453,49 @@ void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64
 
 extern "C" {
 
+smat_status smat_csr_to_bcsr_split_host(const smat_csr* A, int32_t block_cols, const int64_t* row_perm,
+                                        int64_t* n_24, int64_t* n_dense, int32_t* row_ptr_24, int32_t* col_idx_24,
+                                        uint16_t* values_24, int32_t* row_ptr_dense, int32_t* col_idx_dense,
+                                        uint16_t* values_dense, int32_t* block_info) {
+  if (!A || !n_24 || !n_dense) return fail(SMAT_ERR_INVALID, "null argument");
+  HostBcsr b;
+  smat_status st = build_host_bcsr(*A, 16, block_cols, row_perm, b);
+  if (st != SMAT_OK) return st;
+  std::vector<int8_t> info;
+  block_info_ref(*A, row_perm, b, info);
+  const int64_t nbr = b.nbr(), nbc = b.cols_p / b.bw, bsz = 16 * (int64_t)b.bw;
+  int64_t c24 = 0, cd = 0;
+  for (int8_t v : info) (v == 1 ? c24 : cd)++;
+  *n_24 = c24;
+  *n_dense = cd;
+  if (block_info) {
+    std::fill(block_info, block_info + nbr * nbc, 0);
+    for (int64_t br = 0; br < nbr; br++)
+      for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) block_info[br * nbc + b.colidx[k] / b.bw] = info[k];
+  }
+  if (!row_ptr_24) return SMAT_OK;
+  int64_t i24 = 0, id = 0;
+  row_ptr_24[0] = 0;
+  if (row_ptr_dense) row_ptr_dense[0] = 0;
+  for (int64_t br = 0; br < nbr; br++) {
+    for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) {
+      if (info[k] == 1) {
+        if (col_idx_24) col_idx_24[i24] = b.colidx[k];
+        if (values_24) std::copy(b.val_f16.begin() + k * bsz, b.val_f16.begin() + (k + 1) * bsz, values_24 + i24 * bsz);
+        i24++;
+      } else {
+        if (col_idx_dense) col_idx_dense[id] = b.colidx[k];
+        if (values_dense)
+          std::copy(b.val_f16.begin() + k * bsz, b.val_f16.begin() + (k + 1) * bsz, values_dense + id * bsz);
+        id++;
+      }
+    }
+    row_ptr_24[br + 1] = (int32_t)i24;
+    if (row_ptr_dense) row_ptr_dense[br + 1] = (int32_t)id;
+  }
+  return SMAT_OK;
+}
+
 smat_status smat_spmm_workspace_size(const smat_bcsr* A, int32_t form, int32_t b_dtype, int64_t N,
                                      size_t* bytes) {
   if (!A || !bytes) return fail(SMAT_ERR_INVALID, "null argument");

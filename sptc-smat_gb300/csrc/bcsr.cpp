@@ -224,6 +224,35 @@ smat_status build_host_bcsr_from_blocks(int64_t rows, int64_t cols, int32_t bh, 
   return SMAT_OK;
 }
 
+smat_status block_info_ref(const smat_csr& A, const int64_t* perm, const HostBcsr& b, std::vector<int8_t>& info) {
+  const int64_t nbr = b.nbr(), nbc = b.cols_p / b.bw;
+  info.assign(b.nnzb(), 0);
+#pragma omp parallel
+  {
+    std::vector<int32_t> where(nbc, -1);
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t br = 0; br < nbr; br++) {
+      for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) where[b.colidx[k] / b.bw] = k;
+      for (int64_t r = br * b.bh; r < std::min<int64_t>((br + 1) * b.bh, A.rows); r++) {
+        const int64_t src = perm ? perm[r] : r, j0 = A.row_ptr[src], j1 = A.row_ptr[src + 1];
+        for (int64_t j = j0; j < j1; j++) {
+          const int64_t col = A.col_idx[j];
+          int8_t& st = info[where[col / b.bw]];
+          if (st == 0) {
+            st = 1;  // first entry: the block starts as 2:4
+          } else if (st == 1) {
+            const int64_t q = col % 4;
+            if ((q == 2 || q == 3) && j >= j0 + 2 && A.col_idx[j - 1] == col - 1 && A.col_idx[j - 2] == col - 2)
+              st = 2;  // three consecutive columns in file order: dense
+          }
+        }
+      }
+      for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) where[b.colidx[k] / b.bw] = -1;
+    }
+  }
+  return SMAT_OK;
+}
+
 // Nearest e4m3 value (round to nearest even) of a in [0, 464).
 static inline float e4m3_round(float a) {
   if (a < 0.015625f) return std::nearbyint(a * 512.0f) * (1.0f / 512.0f);  // subnormals: step 2^-9

@@ -78,6 +78,11 @@ struct Plan {
 
 smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);
 
+// The reference's per-block sparsity label (csrToBcsr, matrix.h:679-711), per
+// BCSR block: 1 = "2:4" (the default), 2 = dense once a row of the block has
+// three consecutive columns (file order) ending at column % 4 in {2, 3}.
+smat_status block_info_ref(const smat_csr& A, const int64_t* perm, const HostBcsr& b, std::vector<int8_t>& info);
+
 // FP8 form: per block (BCSR order) the e4m3 codes of value / scale and one
 // FP32 scale, chosen among candidates mapping the block's largest magnitude
 // to 448 ... 224 to minimise the block's squared quantisation error.

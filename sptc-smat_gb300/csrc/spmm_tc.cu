@@ -106,7 +106,7 @@ struct Cfg {
   static_assert(BH == 16 || BH == 32, "block height");
   static_assert(R <= 32, "slot field is 5 bits");
   static_assert(SB <= kStageMaxBlocks, "position field is 5 bits, header sized for 16 entries");
-  static_assert(kStageTiles == NPROD, "one copy warp per tile slot");
+  static_assert(kStageTiles <= 2 * NPROD, "a copy warp issues at most two copies per stage");
   static_assert(NS_FIT >= 2, "two stages must fit");
   static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
   static_assert(!FP8 || (BH == 16 && NSUB == 1), "FP8 form: 16 x 16 blocks, 128-column tiles");
@@ -239,9 +239,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     // ---------------------------------------------------------------- copies
     // Stage number c (counted over the CTA's whole run) needs 1 + ntiles
     // bulk copies: copy 0 = the A blocks and the MMA list, copy j = B tile
-    // j - 1. Copy warp p issues the copies j with (j + c) % 8 == p, so every
-    // warp issues about one copy per stage and the A copy (from HBM, the
-    // slowest) rotates. A warp keeps only about one copy at a time in flight,
+    // j - 1. Copy warp p issues the copies j with (j + c) % 8 == p (j and
+    // j + 8), so every warp issues one or two copies per stage and the A
+    // copy (from HBM, the slowest) rotates. A warp keeps only about one copy at a time in flight,
     // so spreading them is what keeps the copy engine busy. The warp that
     // issues copy 0 posts the stage's total byte count (arrive.expect_tx) on
     // the stage's full barrier; the others only add their bytes as they land.
@@ -286,13 +286,13 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               off1 = pf_off;
               bytes1 = pf_bytes;
               total = bytes1 + ntl * (int)C::TILEB;
-              if (ntl == kStageTiles) {
-                has2 = 1;
-                off2 = ((int64_t)rp->kb[kStageTiles - 1] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
-              }
             } else if (j0 <= ntl) {
               off1 = ((int64_t)rp->kb[j0 - 1] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
               bytes1 = (int)C::TILEB;
+            }
+            if (j0 + 8 <= ntl) {  // the warp's second copy: tile j0 + 7
+              has2 = 1;
+              off2 = ((int64_t)rp->kb[j0 + 7] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
             }
           }
           // A comes from HBM: prefetch each stage's A region into L2 kPrefetchAhead
@@ -332,12 +332,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
                   *reinterpret_cast<uint32_t*>(smem + s * C::STAGE + C::OFF_HW) = (uint32_t)hw;
                   mbar_arrive_expect_tx(fb, (uint32_t)tot);
                   bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), P.aval + o1, (uint32_t)b1, fb, pol_a);
-                  if (h2)
-                    bulk_load_hint(st + C::OFF_B + (kStageTiles - 1) * C::TILEB, P.bpack + o2, C::TILEB, fb,
-                                   pol_b);
                 } else {
                   bulk_load_hint(st + C::OFF_B + (j - 1) * C::TILEB, P.bpack + o1, C::TILEB, fb, pol_b);
                 }
+                if (h2) bulk_load_hint(st + C::OFF_B + (j + 7) * C::TILEB, P.bpack + o2, C::TILEB, fb, pol_b);
                 if (b1 != 0) last_mine = ci;
               } else {
                 good = 0;

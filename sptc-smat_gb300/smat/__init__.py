@@ -166,6 +166,33 @@ def csr_to_bcsr_host(csr: Csr, block=(16, 16), row_perm=None):
     return rp, ci[:n], vals[: n * bh * bw].view(np.float16).reshape(n, bh, bw)
 
 
+def csr_to_bcsr_split_host(csr: Csr, block_cols: int = 16, row_perm=None):
+    """The reference's 2:4 / dense block split (smat_csr_to_bcsr_split_host):
+    ((row_ptr, col_idx, values) of the "2:4" blocks, the same of the dense
+    blocks, the label grid)."""
+    perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
+    s = csr.struct()
+    n24, nd = C.c_int64(), C.c_int64()
+    pp = None if perm is None else perm.ctypes.data
+    check(lib().smat_csr_to_bcsr_split_host(C.byref(s), block_cols, pp, C.byref(n24), C.byref(nd), None, None, None,
+                                            None, None, None, None))
+    nbr = (csr.rows + 15) // 16
+    nbc = (csr.cols + block_cols - 1) // block_cols
+    bsz = 16 * block_cols
+    out = []
+    for n in (n24.value, nd.value):
+        out.append((np.zeros(nbr + 1, np.int32), np.zeros(max(n, 1), np.int32), np.zeros(max(n, 1) * bsz, np.uint16)))
+    grid = np.zeros(max(nbr * nbc, 1), np.int32)
+    (a_rp, a_ci, a_v), (d_rp, d_ci, d_v) = out
+    check(lib().smat_csr_to_bcsr_split_host(C.byref(s), block_cols, pp, C.byref(n24), C.byref(nd), a_rp.ctypes.data,
+                                            a_ci.ctypes.data, a_v.ctypes.data, d_rp.ctypes.data, d_ci.ctypes.data,
+                                            d_v.ctypes.data, grid.ctypes.data))
+    n1, n2 = n24.value, nd.value
+    return ((a_rp, a_ci[:n1], a_v[:n1 * bsz].view(np.float16).reshape(n1, 16, block_cols)),
+            (d_rp, d_ci[:n2], d_v[:n2 * bsz].view(np.float16).reshape(n2, 16, block_cols)),
+            grid[:nbr * nbc].reshape(nbr, nbc))
+
+
 def _torch_dt(dt):
     import torch
     return {torch.float32: F32, torch.float16: F16, torch.bfloat16: BF16}[dt]

@@ -79,6 +79,9 @@ _SIGS = {
     "smat_bcsr_export": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "smat_csr_to_bcsr_host": (C.c_int, [C.POINTER(CsrStruct), C.c_int32, C.c_int32, C.c_void_p,
                                          C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smat_csr_to_bcsr_split_host": (C.c_int, [C.POINTER(CsrStruct), C.c_int32, C.c_void_p, C.POINTER(C.c_int64),
+                                              C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p]),
     "smat_spmm_workspace_size": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
     "smat_spmm": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                             C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_size_t, C.c_void_p]),

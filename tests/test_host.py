@@ -157,3 +157,26 @@ def test_partition_rows_covers_all_rows(smat_mod):
         assert parts[0][0] == 0 and parts[-1][1] == A.rows
         assert all(p[1] == q[0] for p, q in zip(parts, parts[1:]))
         assert all(p[0] % 16 == 0 for p in parts)
+
+
+def test_block_split_matches_reference_labels(smat_mod):
+    """smat_csr_to_bcsr_split_host: the reference's blockInfo labels
+    (csrToBcsr, frozen in golden_bcsr.npz) and its filterBcsrBlocks split."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_bcsr.npz"))
+    for i in range(int(g["bcsr_n"])):
+        mr, mc, k = (int(x) for x in g[f"bcsr{i}_dims"])
+        A = smat_mod.Csr(mr, mc, g[f"bcsr{i}_rowptr"].astype(np.int64), g[f"bcsr{i}_cols"],
+                         g[f"bcsr{i}_vals"].astype(np.float16))
+        (rp24, ci24, v24), (rpd, cid, vd), grid = smat_mod.csr_to_bcsr_split_host(A, block_cols=k)
+        assert np.array_equal(grid.reshape(-1), g[f"bcsr{i}_info"]), i
+        brp, bci = g[f"bcsr{i}_brp"], g[f"bcsr{i}_bci"]
+        bval = g[f"bcsr{i}_bval"].view(np.uint16).reshape(-1, 16, k)
+        nbc = mc // k
+        lab = np.array([grid[r, c // k] for r in range(len(brp) - 1) for c in bci[brp[r]:brp[r + 1]]])
+        for want, (rp, ci, v) in ((1, (rp24, ci24, v24)), (2, (rpd, cid, vd))):
+            sel = lab == want
+            assert np.array_equal(ci, bci[sel]), (i, want)
+            assert np.array_equal(v.view(np.uint16), bval[sel]), (i, want)
+            rows = np.repeat(np.arange(len(brp) - 1), np.diff(brp))[sel]
+            assert np.array_equal(rp, np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=len(brp) - 1))])), i
