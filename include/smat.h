@@ -79,6 +79,11 @@ typedef struct smat_bcsr_opts {
   float split_frac;       /* a panel costing more than split_frac x the average per-CTA
                              work is split into parts over several CTAs (0 = default 1.0,
                              < 0 = never split) */
+  const int64_t* col_perm;/* (host, optional) new column c = old column col_perm[c]: A is
+                             blocked with its columns permuted (the reference's column
+                             reordering, src/reorder.py:140-182) and smat_spmm gathers B's
+                             rows through the same permutation, so C = A * B unchanged;
+                             smat_bcsr_export then shows the permuted columns */
 } smat_bcsr_opts;
 
 typedef struct smat_bcsr smat_bcsr; /* opaque handle, immutable after create */

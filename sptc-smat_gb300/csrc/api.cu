@@ -66,12 +66,16 @@ static void free_handle(smat_bcsr* h) {
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
-  void* ptrs[] = {h->d_row_map, h->d_stages, h->d_panels,
-                  h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
-                  h->d_bstage, h->d_cstage, h->d_ws, h->sched[1].d_cta_ptr, h->sched[1].d_cta_items,
-                  h->sched[1].d_items, h->sched[2].d_cta_ptr, h->sched[2].d_cta_items, h->sched[2].d_items};
+  void* ptrs[] = {h->d_row_map, h->d_kperm, h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
+                  h->d_bstage, h->d_cstage, h->d_ws};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (PlanDev& pd : h->pc) {
+    void* pp[] = {pd.d_stages, pd.d_panels, pd.sched[1].d_cta_ptr, pd.sched[1].d_cta_items, pd.sched[1].d_items,
+                  pd.sched[2].d_cta_ptr, pd.sched[2].d_cta_items, pd.sched[2].d_items};
+    for (void* p : pp)
+      if (p) cudaFree(p);
+  }
   if (prev >= 0) cudaSetDevice(prev);
   delete h;
 }
@@ -82,7 +86,7 @@ int smat::kind_of(int32_t form) {
 }
 
 int smat::pick_nsub(const smat_bcsr* h, int64_t N, int kind) {
-  if (N > 128 && kind == TC_KIND_PLAIN && tc_variant_supported(h->host.bh, h->plan.R, 2, kind)) return 2;
+  if (N > 128 && kind == TC_KIND_PLAIN && tc_variant_supported(h->host.bh, h->R, 2, kind)) return 2;
   return 1;
 }
 
@@ -113,10 +117,17 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     delete h;
     return fail(SMAT_ERR_UNSUPPORTED, "unsupported panel_rows for this block height");
   }
-  st = build_plan(h->host, R, h->plan);
-  if (st != SMAT_OK) {
-    delete h;
-    return st;
+  h->R = R;
+  // class 0 serves the FP16, BF16 and FP8 forms (and the handle's info);
+  // class 1 the split form
+  for (int cls = 0; cls < kPlanClasses; cls++) {
+    if (cls == 1 && !(forms & (1u << SMAT_FORM_SPLIT_BF16))) continue;
+    st = build_plan(h->host, R, cls, h->pc[cls].plan);
+    if (st != SMAT_OK) {
+      delete h;
+      return st;
+    }
+    h->pc[cls].built = true;
   }
   for (uint8_t v : h->host.is24) h->n_24 += v;
   if (!h->use24) h->n_24 = 0;
@@ -131,31 +142,35 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   } while (0)
 
   const HostBcsr& b = h->host;
-  const Plan& pl = h->plan;
   SMAT_TRY(upload(&h->d_row_map, b.row_map.data(), b.row_map.size()));
-  SMAT_TRY(upload(&h->d_stages, pl.stages.data(), pl.stages.size()));
-  SMAT_TRY(upload(&h->d_panels, pl.panels.data(), pl.panels.size()));
+  if (!b.kperm.empty()) SMAT_TRY(upload(&h->d_kperm, b.kperm.data(), b.kperm.size()));
   {
     int zero = 0;
     SMAT_TRY(upload(&h->d_err, &zero, 1));
   }
-
-  // work items per launch shape (NSUB 1 and 2): heavy panels split into
-  // parts so that no CTA gets much more than the average
-  for (int nsub = 1; nsub <= 2; nsub++) {
-    if (!tc_variant_supported(bh, R, nsub, TC_KIND_PLAIN)) continue;
-    const int per_sm = tc_ctas_per_sm(bh, R, nsub, TC_KIND_PLAIN);
-    const int workers = std::max(1, h->num_sms * per_sm);
-    std::vector<WorkItem> items;
-    std::vector<int32_t> cta_ptr, cta_items;
-    Sched& sc = h->sched[nsub];
-    const double frac = split_frac == 0.0f ? 1.0 : (split_frac < 0.0f ? 1e30 : (double)split_frac);
-    build_work_items(pl, bh, workers, frac, items, cta_ptr, cta_items, sc.n_split, sc.n_slabs);
-    sc.grid = std::max(1, std::min<int>(workers, (int)items.size()));
-    cta_ptr.resize(sc.grid + 1);  // queues past the item count are empty
-    SMAT_TRY(upload(&sc.d_items, items.data(), items.size()));
-    SMAT_TRY(upload(&sc.d_cta_ptr, cta_ptr.data(), cta_ptr.size()));
-    SMAT_TRY(upload(&sc.d_cta_items, cta_items.data(), cta_items.size()));
+  const double frac = split_frac == 0.0f ? 1.0 : (split_frac < 0.0f ? 1e30 : (double)split_frac);
+  for (int cls = 0; cls < kPlanClasses; cls++) {
+    PlanDev& pd = h->pc[cls];
+    if (!pd.built) continue;
+    SMAT_TRY(upload(&pd.d_stages, pd.plan.stages.data(), pd.plan.stages.size()));
+    SMAT_TRY(upload(&pd.d_panels, pd.plan.panels.data(), pd.plan.panels.size()));
+    // work items per launch shape (NSUB 1 and 2): heavy panels split into
+    // parts so that no CTA gets much more than the average
+    const int kind = cls == 1 ? TC_KIND_SPLIT : TC_KIND_PLAIN;
+    for (int nsub = 1; nsub <= 2; nsub++) {
+      if (!tc_variant_supported(bh, R, nsub, kind)) continue;
+      const int per_sm = tc_ctas_per_sm(bh, R, nsub, kind);
+      const int workers = std::max(1, h->num_sms * per_sm);
+      std::vector<WorkItem> items;
+      std::vector<int32_t> cta_ptr, cta_items;
+      Sched& sc = pd.sched[nsub];
+      build_work_items(pd.plan, bh, workers, frac, items, cta_ptr, cta_items, sc.n_split, sc.n_slabs);
+      sc.grid = std::max(1, std::min<int>(workers, (int)items.size()));
+      cta_ptr.resize(sc.grid + 1);  // queues past the item count are empty
+      SMAT_TRY(upload(&sc.d_items, items.data(), items.size()));
+      SMAT_TRY(upload(&sc.d_cta_ptr, cta_ptr.data(), cta_ptr.size()));
+      SMAT_TRY(upload(&sc.d_cta_items, cta_items.data(), cta_items.size()));
+    }
   }
 
   // A streams, one per requested form: for each stage its blocks in
@@ -165,9 +180,9 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   // stage header.
   const int64_t nnzb = b.nnzb();
   const size_t bsz = (size_t)bh * bw, ablk = (size_t)bh * 32;
-  const int64_t nst = (int64_t)pl.stages.size();
-  auto stream_layout = [&](const std::vector<uint16_t>& hi, const std::vector<uint16_t>* lo,
+  auto stream_layout = [&](const Plan& pl, const std::vector<uint16_t>& hi, const std::vector<uint16_t>* lo,
                            std::vector<uint8_t>& out) {
+    const int64_t nst = (int64_t)pl.stages.size();
     const size_t nops = lo ? 2 : 1;
     out.assign(std::max<size_t>((size_t)nnzb * ablk * nops + pl.headers.size(), 16), 0);
     auto put = [&](const std::vector<uint16_t>& vals, int64_t k, uint8_t* dst) {
@@ -190,7 +205,7 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   std::vector<uint8_t> lay;
   const size_t nval = (size_t)nnzb * bsz;
   if (forms & (1u << SMAT_FORM_F16)) {
-    stream_layout(b.val_f16, nullptr, lay);
+    stream_layout(h->pc[0].plan, b.val_f16, nullptr, lay);
     SMAT_TRY(upload(&h->d_aval[SMAT_FORM_F16], lay.data(), lay.size()));
   }
   if (forms & ((1u << SMAT_FORM_BF16) | (1u << SMAT_FORM_SPLIT_BF16))) {
@@ -200,11 +215,11 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
       lo[i] = f32_to_bf16_bits(b.val[i] - bf16_bits_to_f32(hi[i]));
     }
     if (forms & (1u << SMAT_FORM_BF16)) {
-      stream_layout(hi, nullptr, lay);
+      stream_layout(h->pc[0].plan, hi, nullptr, lay);
       SMAT_TRY(upload(&h->d_aval[SMAT_FORM_BF16], lay.data(), lay.size()));
     }
     if (forms & (1u << SMAT_FORM_SPLIT_BF16)) {
-      stream_layout(hi, &lo, lay);
+      stream_layout(h->pc[1].plan, hi, &lo, lay);
       SMAT_TRY(upload(&h->d_aval[SMAT_FORM_SPLIT_BF16], lay.data(), lay.size()));
     }
   }
@@ -214,6 +229,8 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
       return fail(SMAT_ERR_UNSUPPORTED, "FP8 form: 16 x 16 blocks only");
     }
     SMAT_TRY(quantize_fp8(b, h->fp8_q, h->fp8_scale));
+    const Plan& pl = h->pc[0].plan;
+    const int64_t nst = (int64_t)pl.stages.size();
     // per stage: [nblk e4m3 blocks][nblk FP32 scales, padded][header]
     lay.assign(std::max<size_t>((size_t)nnzb * 256 + pl.headers.size() +
                                     (nst ? (size_t)pl.stages[nst - 1].scl_off + fp8_scale_bytes(pl.stages[nst - 1].nblk) : 0),
@@ -317,7 +334,33 @@ smat_status smat_bcsr_create(const smat_csr* A, const smat_bcsr_opts* opts, smat
   smat_status st = new_handle(o, forms, &h);
   if (st != SMAT_OK) return st;
   DeviceGuard guard(o.device);
-  st = build_host_bcsr(*A, bh, bw, o.row_perm, h->host);
+  if (o.col_perm) {
+    // block the matrix with its columns permuted: new column inv[old]
+    std::vector<int32_t> inv(std::max<int64_t>(A->cols, 0), -1);
+    for (int64_t c = 0; c < A->cols; c++) {
+      const int64_t src = o.col_perm[c];
+      if (src < 0 || src >= A->cols || inv[src] >= 0) {
+        delete h;
+        return fail(SMAT_ERR_INVALID, "col_perm is not a permutation");
+      }
+      inv[src] = (int32_t)c;
+    }
+    std::vector<int32_t> ci(std::max<int64_t>(A->nnz, 0));
+    for (int64_t k = 0; k < A->nnz; k++) {
+      const int32_t c = A->col_idx[k];
+      if (c < 0 || c >= A->cols) {
+        delete h;
+        return fail(SMAT_ERR_INVALID, "column index out of range");
+      }
+      ci[k] = inv[c];
+    }
+    smat_csr A2 = *A;
+    A2.col_idx = ci.data();
+    st = build_host_bcsr(A2, bh, bw, o.row_perm, h->host);
+    h->host.kperm.assign(o.col_perm, o.col_perm + A->cols);
+  } else {
+    st = build_host_bcsr(*A, bh, bw, o.row_perm, h->host);
+  }
   if (st != SMAT_OK) {
     delete h;
     return st;
@@ -371,11 +414,11 @@ smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info) {
   info->n_blocks_24 = A->n_24;
   info->block_rows = b.bh;
   info->block_cols = b.bw;
-  info->panel_rows = A->plan.R;
-  info->n_panels = A->plan.n_panels;
+  info->panel_rows = A->R;
+  info->n_panels = A->pc[0].plan.n_panels;
   {
     int64_t u = 0;
-    for (const auto& p : A->plan.panels) u += p.nucol;
+    for (const auto& p : A->pc[0].plan.panels) u += p.nucol;
     info->n_union_cols = u;
   }
   info->fill = b.nnzb() ? (double)b.nnz / ((double)b.nnzb() * b.bh * b.bw) : 0.0;
@@ -416,11 +459,11 @@ WsLayout smat::ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
   const size_t one = (packed_b_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
   w.counters = split ? 2 * one : one;
   const int nsub = pick_nsub(A, N, kind_of(form));
-  const Sched& sc = A->sched[nsub];
+  const Sched& sc = A->pc[plan_class(form)].sched[nsub];
   const int64_t bn = 128 * nsub, n_tiles = (std::max<int64_t>(N, 1) + bn - 1) / bn;
   w.counter_bytes = ((size_t)sc.n_split * n_tiles * 4 * sizeof(int32_t) + 255) / 256 * 256;
   w.slabs = w.counters + w.counter_bytes;
-  w.total = w.slabs + (size_t)sc.n_slabs * n_tiles * A->plan.R * A->host.bh * bn * sizeof(float);
+  w.total = w.slabs + (size_t)sc.n_slabs * n_tiles * A->R * A->host.bh * bn * sizeof(float);
   return w;
 }
 
@@ -434,8 +477,8 @@ void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64
   P.bpack = ws;
   P.bp_ntiles = packed_b_tiles(N);
   P.aval = A->d_aval[form];
-  P.panels = A->d_panels;
-  P.stages = A->d_stages;
+  P.panels = A->pc[plan_class(form)].d_panels;
+  P.stages = A->pc[plan_class(form)].d_stages;
   P.row_map = A->d_row_map;
   P.C = C;
   P.ldc = ldc;
@@ -534,7 +577,7 @@ smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, in
   uint8_t* out = static_cast<uint8_t*>(workspace);
   const int in_dt = b_dtype == SMAT_F32 ? 0 : (b_dtype == SMAT_F16 ? 1 : 2);
   const int mode = (form == SMAT_FORM_F16 || form == SMAT_FORM_FP8) ? 0 : (split ? 2 : 1);
-  cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, out, K, N,
+  cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, out, K, N, A->d_kperm,
                          static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "pack_b");
   return SMAT_OK;
@@ -553,9 +596,9 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   if (!guard.ok) return fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
   const int kind = kind_of(form);
   const int nsub = pick_nsub(A, N, kind);
-  const int bh = hb.bh, R = A->plan.R;
+  const int bh = hb.bh, R = A->R;
   if (!tc_variant_supported(bh, R, nsub, kind)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
-  const Sched& sc = A->sched[nsub];
+  const Sched& sc = A->pc[plan_class(form)].sched[nsub];
   SpmmArgs args;
   std::memset(&args, 0, sizeof(args));
   const WsLayout wl = ws_layout(A, form, N);

@@ -305,14 +305,15 @@ smat_status quantize_fp8(const HostBcsr& b, std::vector<uint8_t>& q, std::vector
   return SMAT_OK;
 }
 
-smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
+smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
   if (R < 1 || R > 32) return fail(SMAT_ERR_INVALID, "panel rows must be in [1, 32]");
   const int64_t nbr = b.nbr();
   plan.R = R;
   plan.n_panels = (int32_t)((nbr + R - 1) / R);
   const int32_t P = plan.n_panels;
   if (b.nnzb() >= ((int64_t)1 << 31) - 1) return fail(SMAT_ERR_UNSUPPORTED, "too many blocks");
-  const int32_t SB = kStageRows / b.bh;                      // blocks per stage
+  const int32_t SB = stage_rows(cls) / b.bh;                 // blocks per stage
+  const int32_t ST = stage_tiles(cls);                       // B tiles per stage
   const int32_t max_len = std::min<int32_t>(16, kMaxGroupN / b.bh);
   // MMA-issuing warp owning a slot: kMmaWarps equal ranges of slots
   auto owner = [R](uint32_t slot) -> uint32_t { return (uint32_t)((slot * kMmaWarps) / (uint32_t)R); };
@@ -356,7 +357,7 @@ smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan) {
       while (t < ent.size()) {
         StageRec s{};
         mma.clear();
-        while (t < ent.size() && s.ntiles < kStageTiles && s.nblk < SB) {
+        while (t < ent.size() && s.ntiles < ST && s.nblk < SB) {
           const int64_t col = ent[t].first / 32;
           size_t e = t;
           while (e < ent.size() && ent[e].first / 32 == col) e++;

@@ -66,12 +66,13 @@ __device__ __forceinline__ float vec_elem<__nv_bfloat16>(const uint4* v, int i) 
 // read as 16-byte vectors where they are aligned and inside K.
 template <typename T, int OUT>
 __device__ __forceinline__ void pack_tile(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ out,
-                                          int64_t K, int64_t N, int ntiles, int64_t kb, int t, int r) {
+                                          int64_t K, int64_t N, int ntiles, int64_t kb, int t, int r,
+                                          const int32_t* __restrict__ kperm) {
   const int64_t n = (int64_t)t * 128 + r;
   constexpr int VEC = 16 / sizeof(T);  // elements per 16-byte vector
   float xv[16];
   const T* colp = in + kb * 16 + n * ldi;
-  if (layout == 1 && n < N && kb * 16 + 16 <= K && (reinterpret_cast<uintptr_t>(colp) & 15) == 0) {
+  if (!kperm && layout == 1 && n < N && kb * 16 + 16 <= K && (reinterpret_cast<uintptr_t>(colp) & 15) == 0) {
     uint4 v[16 / VEC];
 #pragma unroll
     for (int q = 0; q < 16 / VEC; q++) v[q] = __ldg(reinterpret_cast<const uint4*>(colp) + q);
@@ -81,7 +82,8 @@ __device__ __forceinline__ void pack_tile(const T* __restrict__ in, int layout, 
 #pragma unroll
     for (int i = 0; i < 16; i++) {
       const int64_t k = kb * 16 + i;
-      xv[i] = (k < K && n < N) ? load_f<T>(layout == 1 ? in + k + n * ldi : in + k * ldi + n) : 0.0f;
+      const int64_t ks = (k < K && kperm) ? (int64_t)kperm[k] : k;  // row of B feeding permuted column k
+      xv[i] = (k < K && n < N) ? load_f<T>(layout == 1 ? in + ks + n * ldi : in + ks * ldi + n) : 0.0f;
     }
   }
   uint16_t h[16], l[16];
@@ -111,8 +113,8 @@ __device__ __forceinline__ void pack_tile(const T* __restrict__ in, int layout, 
 
 template <typename T, int OUT>
 __global__ void pack_b_tiles(const T* __restrict__ in, int layout, int64_t ldi, uint8_t* __restrict__ out,
-                             int64_t K, int64_t N, int ntiles) {
-  pack_tile<T, OUT>(in, layout, ldi, out, K, N, ntiles, blockIdx.y, blockIdx.x, threadIdx.x);
+                             int64_t K, int64_t N, int ntiles, const int32_t* __restrict__ kperm) {
+  pack_tile<T, OUT>(in, layout, ldi, out, K, N, ntiles, blockIdx.y, blockIdx.x, threadIdx.x, kperm);
 }
 
 // Many B operands in one launch: block g packs tile (kb, t) of the job whose
@@ -130,9 +132,9 @@ __global__ void pack_b_grouped_kernel(const PackJob* __restrict__ jobs, int njob
     const int t = (int)(local % j.ntiles);
 #define SMAT_GPACK(T)                                                                                        \
   switch (j.out_mode) {                                                                                      \
-    case OUT_F16: pack_tile<T, OUT_F16>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x); break; \
-    case OUT_BF16: pack_tile<T, OUT_BF16>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x); break; \
-    default: pack_tile<T, OUT_SPLIT>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x); break; \
+    case OUT_F16: pack_tile<T, OUT_F16>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x, j.kperm); break; \
+    case OUT_BF16: pack_tile<T, OUT_BF16>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x, j.kperm); break; \
+    default: pack_tile<T, OUT_SPLIT>((const T*)j.in, j.layout, j.ldi, j.out, j.K, j.N, j.ntiles, kb, t, threadIdx.x, j.kperm); break; \
   }
     switch (j.in_dtype) {
       case 0: SMAT_GPACK(float) break;
@@ -154,22 +156,22 @@ __global__ void pack_b_colmajor(const T* __restrict__ in, int64_t ldi, uint8_t* 
   const int64_t kb = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
   const int64_t n = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
   if (kb >= kbs || n >= (int64_t)ntiles * 128) return;
-  pack_tile<T, OUT>(in, 1, ldi, out, K, N, ntiles, kb, (int)(n >> 7), (int)(n & 127));
+  pack_tile<T, OUT>(in, 1, ldi, out, K, N, ntiles, kb, (int)(n >> 7), (int)(n & 127), nullptr);
 }
 
 template <typename T, int OUT>
 static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* out, int64_t K, int64_t N,
-                            cudaStream_t s) {
+                            const int32_t* kperm, cudaStream_t s) {
   const int ntiles = (int)packed_b_tiles(N);
   const int64_t kbs = (K + 15) / 16;
   if (kbs == 0 || ntiles == 0) return cudaSuccess;
-  if (layout == 1 && ((reinterpret_cast<uintptr_t>(in) | (uint64_t)ldi * sizeof(T)) & 15) == 0) {
+  if (!kperm && layout == 1 && ((reinterpret_cast<uintptr_t>(in) | (uint64_t)ldi * sizeof(T)) & 15) == 0) {
     dim3 grid((unsigned)((kbs + 31) / 32), (unsigned)((int64_t)ntiles * 128 / 8));
     pack_b_colmajor<T, OUT><<<grid, 256, 0, s>>>((const T*)in, ldi, out, K, N, ntiles, kbs);
     return cudaGetLastError();
   }
   dim3 grid((unsigned)ntiles, (unsigned)kbs);
-  pack_b_tiles<T, OUT><<<grid, 128, 0, s>>>((const T*)in, layout, ldi, out, K, N, ntiles);
+  pack_b_tiles<T, OUT><<<grid, 128, 0, s>>>((const T*)in, layout, ldi, out, K, N, ntiles, kperm);
   return cudaGetLastError();
 }
 
@@ -185,13 +187,13 @@ size_t packed_b_bytes(int64_t K, int64_t N) {
 }
 
 cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* out,
-                   int64_t K, int64_t N, cudaStream_t s) {
+                   int64_t K, int64_t N, const int32_t* kperm, cudaStream_t s) {
   using namespace dev;
 #define SMAT_PACK(T)                                                                  \
   switch (out_mode) {                                                                 \
-    case OUT_F16: return run_pack<T, OUT_F16>(in, layout, ldi, out, K, N, s);     \
-    case OUT_BF16: return run_pack<T, OUT_BF16>(in, layout, ldi, out, K, N, s);   \
-    case OUT_SPLIT: return run_pack<T, OUT_SPLIT>(in, layout, ldi, out, K, N, s); \
+    case OUT_F16: return run_pack<T, OUT_F16>(in, layout, ldi, out, K, N, kperm, s);     \
+    case OUT_BF16: return run_pack<T, OUT_BF16>(in, layout, ldi, out, K, N, kperm, s);   \
+    case OUT_SPLIT: return run_pack<T, OUT_SPLIT>(in, layout, ldi, out, K, N, kperm, s); \
     default: return cudaErrorInvalidValue;                                            \
   }
   switch (in_dtype) {

@@ -19,8 +19,10 @@ size_t packed_b_bytes(int64_t K, int64_t N);
 // in_dtype: 0 F32, 1 F16, 2 BF16; layout: 0 row-major (k*ldi + n), 1
 // column-major (k + n*ldi); out_mode: 0 FP16, 1 BF16, 2 hi+lo BF16 (8 KB
 // [hi | lo] per tile, twice packed_b_bytes).
+// kperm (device, optional): row kperm[k] of `in` feeds packed row k (a
+// column permutation of A; gathered with scalar loads).
 cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* out,
-                   int64_t K, int64_t N, cudaStream_t s);
+                   int64_t K, int64_t N, const int32_t* kperm, cudaStream_t s);
 
 // One B operand of a grouped pack: tiles of `in` (in_dtype, layout, ldi,
 // K x N) into `out` (out_mode as pack_b), covering global blocks
@@ -28,6 +30,7 @@ cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int ou
 struct PackJob {
   const void* in;
   uint8_t* out;
+  const int32_t* kperm;  // column permutation of A (device), or null
   int64_t ldi, K, N, begin;
   int32_t in_dtype, layout, out_mode, ntiles;
 };

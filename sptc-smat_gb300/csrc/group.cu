@@ -101,9 +101,9 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     if (p.ldc < p.N) return fail(SMAT_ERR_INVALID, "ldc < N");
     const int kind = kind_of(p.form);
     const int nsub = pick_nsub(p.A, p.N, kind);
-    if (!tc_variant_supported(p.A->host.bh, p.A->plan.R, nsub, kind))
+    if (!tc_variant_supported(p.A->host.bh, p.A->R, nsub, kind))
       return fail(SMAT_ERR_UNSUPPORTED, "problem " + std::to_string(i) + ": no kernel variant");
-    variants[{p.A->host.bh, p.A->plan.R, nsub, kind}].push_back(i);
+    variants[{p.A->host.bh, p.A->R, nsub, kind}].push_back(i);
   }
   int prev = -1;
   cudaGetDevice(&prev);
@@ -140,7 +140,7 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     std::vector<const Plan*> plans;
     std::vector<int32_t> bhs;
     for (int32_t i : members) {
-      plans.push_back(&probs[i].A->plan);
+      plans.push_back(&probs[i].A->pc[kind == TC_KIND_SPLIT ? 1 : 0].plan);
       bhs.push_back(probs[i].A->host.bh);
     }
     const int workers = std::max(1, g->num_sms * tc_ctas_per_sm(bh, std::get<1>(kv.first), nsub, kind));
@@ -153,7 +153,7 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
       Scratch& s = sc[members[m]];
       const size_t one = (packed_b_bytes(p.A->host.cols, p.N) + 255) / 256 * 256;
       s.packed = kind == TC_KIND_SPLIT ? 2 * one : one;
-      s.slabs = (size_t)n_slabs[m] * n_tiles * p.A->plan.R * p.A->host.bh * bn * sizeof(float);
+      s.slabs = (size_t)n_slabs[m] * n_tiles * p.A->R * p.A->host.bh * bn * sizeof(float);
       s.ctr_n = (size_t)n_split[m] * n_tiles * 4;
     }
     Launch l;
@@ -190,6 +190,7 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     PackJob& j = jobs[i];
     j.in = p.B;
     j.out = g->d_ws + sc[i].ws_off;
+    j.kperm = p.A->d_kperm;
     j.ldi = p.ldb;
     j.K = p.A->host.cols;
     j.N = p.N;

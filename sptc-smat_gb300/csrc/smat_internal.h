@@ -47,6 +47,7 @@ struct HostBcsr {
   std::vector<uint16_t> val_f16;     // same, as the FP16 the reference stores
   std::vector<int32_t> row_map;      // rows_p: BCSR row -> original row (or -1)
   std::vector<uint8_t> is24;         // per block: exactly 2:4 (values as FP16)
+  std::vector<int32_t> kperm;        // permuted column -> original column (empty: none)
   int64_t nnzb() const { return (int64_t)colidx.size(); }
   int64_t nbr() const { return rows_p / bh; }
 };
@@ -63,7 +64,8 @@ smat_status build_host_bcsr_from_blocks(int64_t rows, int64_t cols, int32_t bh, 
 
 // Work plan of the tensor-core SpMM. Panels of `R` block rows; the blocks of
 // a panel are ordered by block column (then block row) and cut into stages
-// of at most kStageRows / bh blocks and kStageTiles block columns. Each stage
+// of at most stage_rows(cls) / bh blocks and stage_tiles(cls) block columns
+// (cls: the plan class, spmm_tc.h). Each stage
 // has a record (StageRec) and a header with its MMA list (spmm_tc.h).
 struct Plan {
   int32_t R = 8;
@@ -76,7 +78,7 @@ struct Plan {
   int64_t n_tiles = 0;               // B tile loads per pass over A
 };
 
-smat_status build_plan(const HostBcsr& b, int32_t R, Plan& plan);
+smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan);
 
 // The reference's per-block sparsity label (csrToBcsr, matrix.h:679-711), per
 // BCSR block: 1 = "2:4" (the default), 2 = dense once a row of the block has
@@ -109,18 +111,26 @@ struct Sched {
   int32_t n_slabs = 0;  // parts of split panels
 };
 
+// A plan class's plan and its device copies and work lists.
+struct PlanDev {
+  Plan plan;
+  bool built = false;
+  PanelInfo* d_panels = nullptr;
+  StageRec* d_stages = nullptr;
+  Sched sched[3];  // by NSUB (1, 2)
+};
+
 struct SmatBcsrBody {
   int device = 0;
   HostBcsr host;
-  Plan plan;
+  int32_t R = 16;  // block rows per panel
+  PlanDev pc[kPlanClasses];
   uint32_t forms = 0;
   int use24 = 0;
   int64_t n_24 = 0;
   int num_sms = 0;
   int32_t* d_row_map = nullptr;
-  PanelInfo* d_panels = nullptr;
-  StageRec* d_stages = nullptr;
-  Sched sched[3];  // by NSUB (1, 2)
+  int32_t* d_kperm = nullptr;  // column permutation for the B gather (or null)
   // A stream per form (F16, BF16, -, SPLIT): per stage the pre-swizzled
   // blocks in consumption order (hi, then lo for the split form) and the
   // stage header
@@ -146,8 +156,10 @@ struct smat_bcsr : smat::SmatBcsrBody {};
 
 namespace smat {
 
-// Kernel kind of an arithmetic form, and the N-tile width (128 * nsub) used for N.
+// Kernel kind of an arithmetic form, its plan class, and the N-tile width
+// (128 * nsub) used for N.
 int kind_of(int32_t form);
+inline int plan_class(int32_t form) { return form == SMAT_FORM_SPLIT_BF16 ? 1 : 0; }
 int pick_nsub(const smat_bcsr* h, int64_t N, int kind);
 
 // Workspace layout of one SpMM: [packed B (x2 for the split form)]

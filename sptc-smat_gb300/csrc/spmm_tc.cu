@@ -75,7 +75,10 @@ template <int BH, int R, int NSUB, int KIND>
 struct Cfg {
   static constexpr int BN = 128 * NSUB;                   // C columns per tile
   static constexpr int NOPS = (KIND == KIND_SPLIT) ? 2 : 1;
-  static constexpr int SB = kStageRows / BH;              // A blocks per stage (at most)
+  static constexpr int CLS = KIND == KIND_SPLIT ? 1 : 0;  // plan class (stage shape)
+  static constexpr int SB = stage_rows(CLS) / BH;         // A blocks per stage (at most)
+  static constexpr int ST = stage_tiles(CLS);             // B tiles per stage (at most)
+  static constexpr int HDRMAX = stage_hdr_max(SB);
   static constexpr uint32_t ABLK = BH * 32;               // bytes of one A block (one operand)
   static constexpr uint32_t TILE = BN * 32;               // bytes of one B tile (one operand)
   static constexpr uint32_t TILEB = TILE * NOPS;          // bytes of one B tile slot
@@ -84,10 +87,10 @@ struct Cfg {
   // FP8 form lands [e4m3 blocks | scales | header] in a staging area after
   // the A blocks, which the converter warps turn into FP16 A blocks
   static constexpr uint32_t OFF_STG = SB * ABLK * NOPS;
-  static constexpr uint32_t STG_BYTES = FP8 ? (SB * 256 + fp8_scale_bytes(SB) + kStageHdrMax + 255) / 256 * 256 : 0;
-  static constexpr uint32_t A_END = FP8 ? OFF_STG + STG_BYTES : OFF_STG + kStageHdrMax;
+  static constexpr uint32_t STG_BYTES = FP8 ? (SB * 256 + fp8_scale_bytes(SB) + HDRMAX + 255) / 256 * 256 : 0;
+  static constexpr uint32_t A_END = FP8 ? OFF_STG + STG_BYTES : OFF_STG + HDRMAX;
   static constexpr uint32_t OFF_B = (A_END + 1023) / 1024 * 1024;
-  static constexpr uint32_t OFF_HW = OFF_B + kStageTiles * TILEB;
+  static constexpr uint32_t OFF_HW = OFF_B + ST * TILEB;
   static constexpr uint32_t STAGE = (OFF_HW + 16 + 1023) / 1024 * 1024;
   static constexpr uint32_t SMEM_AVAIL = 227 * 1024 - 2048;  // minus alignment slack and barriers
   static constexpr int NS_FIT = (int)(SMEM_AVAIL / STAGE);
@@ -105,8 +108,8 @@ struct Cfg {
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
   static_assert(R <= 32, "slot field is 5 bits");
-  static_assert(SB <= kStageMaxBlocks, "position field is 5 bits, header sized for 16 entries");
-  static_assert(kStageTiles <= 2 * NPROD, "a copy warp issues at most two copies per stage");
+  static_assert(SB <= kMaxStageBlocks, "position field is 5 bits");
+  static_assert(ST <= 2 * NPROD && ST <= kMaxStageTiles, "a copy warp issues at most two copies per stage");
   static_assert(NS_FIT >= 2, "two stages must fit");
   static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
   static_assert(!FP8 || (BH == 16 && NSUB == 1), "FP8 form: 16 x 16 blocks, 128-column tiles");

@@ -9,12 +9,18 @@
 
 namespace smat {
 
-// A pipeline STAGE carries up to kStageRows * 16 / bh A blocks of one panel
-// (in the order the kernel consumes them), up to kStageTiles packed B tiles
-// those blocks need, and the stage's MMA list. The limits keep a stage's A
-// part at 8 KB (FP16) and its B part at 32 KB (128-column tiles).
-constexpr int kStageRows = 256;   // A rows per stage: 16 blocks of 16 rows, 8 of 32
-constexpr int kStageTiles = 8;
+// A pipeline STAGE carries up to stage_rows(cls) / bh A blocks of one panel
+// (in the order the kernel consumes them), up to stage_tiles(cls) packed B
+// tiles those blocks need, and the stage's MMA list. There are two stage
+// shapes ("plan classes"): class 0 for the FP16, BF16 and FP8 forms (24
+// blocks of 16 rows and 12 B tiles: 12 KB of A and 48 KB of B, three stages
+// in flight), class 1 for the split form, whose stages hold hi and lo
+// copies of everything (12 blocks and 6 tiles: the same bytes).
+constexpr int kPlanClasses = 2;
+constexpr int kMaxStageTiles = 16;   // StageRec::kb capacity (a copy warp issues at most two copies)
+constexpr int kMaxStageBlocks = 31;  // the entry's position field has 5 bits
+__host__ __device__ constexpr int stage_rows(int cls) { return cls == 0 ? 384 : 192; }
+__host__ __device__ constexpr int stage_tiles(int cls) { return cls == 0 ? 12 : 6; }
 constexpr int kMmaWarps = 4;      // MMA-issuing warps; each owns a quarter of the panel's block rows
 constexpr int kMaxGroupN = 256;   // widest tcgen05.mma N (kind::f16, M = 128)
 
@@ -28,7 +34,7 @@ struct PanelInfo {
   int32_t pad0, pad1, pad2;
 };
 
-// Per-stage record (64 bytes), read by the copy warps. In the device A
+// Per-stage record (96 bytes), read by the copy warps. In the device A
 // stream of a form (ABLK = bh * 32 bytes per block and operand, NOPS = 2 for
 // the split form, else 1) a stage occupies
 //     [nblk * ABLK blocks (hi)][nblk * ABLK blocks (lo, split form only)][header]
@@ -43,9 +49,9 @@ struct StageRec {
   int64_t hdr_off;     // header bytes before this stage
   int32_t nblk;        // A blocks in the stage
   int32_t hdr_bytes;   // bytes of this stage's header (multiple of 16)
-  int32_t ntiles;      // B tiles (distinct block columns) of the stage, 1..kStageTiles
+  int32_t ntiles;      // B tiles (distinct block columns) of the stage, 1..stage_tiles
   int32_t scl_off;     // padded FP8 scale bytes before this stage
-  int32_t kb[kStageTiles];  // k-block (column / 16) of each tile
+  int32_t kb[kMaxStageTiles];  // k-block (column / 16) of each tile
 };
 
 // Padded bytes of the FP32 scales of n FP8 blocks.
@@ -63,9 +69,9 @@ __host__ __device__ constexpr int fp8_scale_bytes(int n) { return (4 * n + 15) /
 //   0-4 position of the first A block in the stage, 5-8 B tile in the stage,
 //   9-13 first slot, 14-17 len - 1, 18 accumulate (else overwrite).
 constexpr int kStageHdrFixed = 16;
-constexpr int kStageMaxBlocks = 16;
 constexpr uint32_t kEntAccBit = 1u << 18;
-constexpr int kStageHdrMax = kStageHdrFixed + 4 * kStageMaxBlocks;  // 80 bytes
+// Largest header of a stage with sb blocks (one entry per block at most).
+__host__ __device__ constexpr int stage_hdr_max(int sb) { return kStageHdrFixed + 4 * sb; }
 
 // A unit of work of one CTA: stages [s0, s1) of a panel. A panel whose
 // stages are split over several items ("parts", for load balance) has a

@@ -25,7 +25,7 @@ from ._lib import (BF16, COL_MAJOR, E4M3, F16, F32, F64, FORM_BF16, FORM_F16, FO
                    ROW_MAJOR, BcsrInfo, BcsrOpts, CsrFile, CsrStruct, Problem, ReorderStats, SmatError, TuneResult,
                    check, lib, ptr)
 
-__all__ = ["Csr", "Bcsr", "Group", "autotune", "features", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
+__all__ = ["Csr", "Bcsr", "Group", "autotune", "features", "transpose", "reorder_columns", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
            "FORM_FP8", "FORM_SPLIT_BF16", "F32", "F16", "BF16", "F64", "E4M3", "ROW_MAJOR", "COL_MAJOR"]
 
 _VAL_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float16): F16, np.dtype(np.float64): F64}
@@ -148,6 +148,24 @@ def reorder(csr: Csr, tau: float = 0.5, col_block: int = 16, row_block: int = 16
     return ReorderResult(perm, grouping, st.comparisons, st.merges)
 
 
+def transpose(csr: Csr) -> Csr:
+    """The transposed pattern (and values), rows in column order."""
+    r = np.repeat(np.arange(csr.rows, dtype=np.int64), np.diff(csr.row_ptr))
+    order = np.argsort(csr.col_idx, kind="stable")
+    rp = np.zeros(csr.cols + 1, np.int64)
+    np.add.at(rp, csr.col_idx.astype(np.int64) + 1, 1)
+    vals = None if csr.values is None else csr.values[order]
+    return Csr(csr.cols, csr.rows, np.cumsum(rp), r[order].astype(np.int32), vals)
+
+
+def reorder_columns(csr: Csr, tau: float = 0.5, col_block: int = 16, row_block: int = 16, row_perm=None) -> np.ndarray:
+    """Column permutation from the reference's second pass (src/reorder.py:140-182):
+    Keeper on the rows of the transposed (row-reordered) matrix; new column c =
+    old column result[c]. Use it as Bcsr(..., col_perm=...)."""
+    A = csr if row_perm is None else csr.permuted(np.asarray(row_perm))
+    return reorder(transpose(A), tau=tau, col_block=col_block, row_block=row_block, algo=5, force_fixed=True).perm
+
+
 def csr_to_bcsr_host(csr: Csr, block=(16, 16), row_perm=None):
     """Host-only blocking: (row_ptr, col_idx (column starts), values fp16 [nnzb, bh, bw])."""
     bh, bw = block
@@ -214,7 +232,7 @@ class Bcsr:
     """A BCSR matrix resident on one GPU (the reference's ``SparseMatrix``)."""
 
     def __init__(self, csr: Csr, block=(16, 16), forms=(FORM_F16,), row_perm=None, panel_rows: int = 0,
-                 device: int = 0, use_24: bool = False, split_frac: float = 0.0):
+                 device: int = 0, use_24: bool = False, split_frac: float = 0.0, col_perm=None):
         o = BcsrOpts()
         o.block_rows, o.block_cols = block
         o.forms = 0
@@ -226,6 +244,8 @@ class Bcsr:
         o.device = device
         o.panel_rows = panel_rows
         o.split_frac = split_frac
+        self._cperm = None if col_perm is None else np.ascontiguousarray(col_perm, np.int64)
+        o.col_perm = None if self._cperm is None else self._cperm.ctypes.data
         h = C.c_void_p()
         s = csr.struct()
         check(lib().smat_bcsr_create(C.byref(s), C.byref(o), C.byref(h)))

@@ -32,7 +32,7 @@ class CsrStruct(C.Structure):
 class BcsrOpts(C.Structure):
     _fields_ = [("block_rows", C.c_int32), ("block_cols", C.c_int32), ("forms", C.c_uint32),
                 ("use_24", C.c_int32), ("row_perm", C.c_void_p), ("device", C.c_int32),
-                ("panel_rows", C.c_int32), ("split_frac", C.c_float)]
+                ("panel_rows", C.c_int32), ("split_frac", C.c_float), ("col_perm", C.c_void_p)]
 
 
 class CsrFile(C.Structure):

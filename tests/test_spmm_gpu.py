@@ -302,3 +302,31 @@ def test_host_entry_with_pinned_buffers(dev, smat_mod, oracle_lib, layout):
     ref = spmm(M, torch.from_numpy(Bh).to(dev), smat_mod.FORM_F16)
     assert np.array_equal(Cp.numpy(), ref)
     assert rel_err(Cp.numpy(), fp64_product(oracle_lib, A, Bh)) <= 1e-3
+
+
+def test_column_permutation_keeps_the_product(dev, smat_mod, oracle_lib):
+    """Blocking with a column permutation (the reference's column reordering):
+    the blocks are those of A with its columns permuted, and C = A * B is
+    unchanged because B's rows are gathered through the same permutation."""
+    from smat import generators as G
+    A = G.rmat(11, 30000, seed=21)
+    q = smat_mod.reorder_columns(A, tau=0.6)
+    assert np.array_equal(np.sort(q), np.arange(A.cols))
+    N = 80
+    Bh = np.random.default_rng(21).uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    M = smat_mod.Bcsr(A, col_perm=q)
+    M0 = smat_mod.Bcsr(A)
+    for layout in ("row", "col"):
+        B = torch.from_numpy(Bh).to(dev)
+        if layout == "col":
+            B = B.t().contiguous().t()
+        got = spmm(M, B, smat_mod.FORM_F16)
+        assert rel_err(got, spmm(M0, B, smat_mod.FORM_F16)) <= 1e-6
+        assert rel_err(got, fp64_product(oracle_lib, A, Bh)) <= 1e-3
+    # the blocks are those of the column-permuted matrix
+    inv = np.empty_like(q)
+    inv[q] = np.arange(q.size)
+    Aq = smat_mod.Csr(A.rows, A.cols, A.row_ptr, inv[A.col_idx], A.values)
+    rp, ci, v = smat_mod.csr_to_bcsr_host(Aq)
+    erp, eci, ev, _ = M.export()
+    assert np.array_equal(rp, erp) and np.array_equal(ci, eci) and np.array_equal(v.view(np.uint16), ev.view(np.uint16))
