@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sptc-smat_gb300"))
 
 METRIC = "SpMM useful TFLOP/s, chosen form vs plain FP16 BCSR on one GB300 at stated rel err"
-CACHE = os.environ.get("SMAT_CACHE", "/tmp/smat_bench_cache")
+CACHE = os.environ.get("SMAT_CACHE", os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "bench_cache"))
 
 WORKLOAD = {
     "workload": "rmat16_2M_reordered_tau0.6_bcsr16x16_24frac0.3_N128",

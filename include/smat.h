@@ -75,7 +75,9 @@ typedef struct smat_bcsr_opts {
   const int64_t* row_perm;/* (host, optional) new row r = old row row_perm[r]; SpMM results
                              are written back in the ORIGINAL row order */
   int32_t device;         /* CUDA device ordinal */
-  int32_t panel_rows;     /* block rows per tensor-core work item (0 = autotuned) */
+  int32_t panel_rows;     /* block rows per tensor-core panel: 4, 8 or 16 for bh 16, 4 or 8
+                             for bh 32; 0 = the autotuner's cached choice for matrices
+                             like this one, else 128 rows (8, or 4 for bh 32) */
   float split_frac;       /* a panel costing more than split_frac x the average per-CTA
                              work is split into parts over several CTAs (0 = default 1.0,
                              < 0 = never split) */

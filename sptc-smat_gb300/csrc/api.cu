@@ -66,12 +66,12 @@ static void free_handle(smat_bcsr* h) {
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
-  void* ptrs[] = {h->d_row_map, h->d_kperm, h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
+  void* ptrs[] = {h->d_kperm, h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
                   h->d_bstage, h->d_cstage, h->d_ws};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (PlanDev& pd : h->pc) {
-    void* pp[] = {pd.d_stages, pd.d_panels, pd.sched[1].d_cta_ptr, pd.sched[1].d_cta_items, pd.sched[1].d_items,
+    void* pp[] = {pd.d_stages, pd.d_panels, pd.d_row_map, pd.sched[1].d_cta_ptr, pd.sched[1].d_cta_items, pd.sched[1].d_items,
                   pd.sched[2].d_cta_ptr, pd.sched[2].d_cta_items, pd.sched[2].d_items};
     for (void* p : pp)
       if (p) cudaFree(p);
@@ -98,9 +98,8 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   const int bh = h->host.bh, bw = h->host.bw;
   const uint32_t forms = h->forms;
   smat_status st;
-  // 16 block rows per panel (8 of 32 rows) fill TMEM's 512 columns with two
-  // accumulator buffers; heavy panels are split over CTAs below
-  int R = o.panel_rows ? o.panel_rows : (bh == 16 ? 16 : 8);
+  // heavy panels are split over CTAs below
+  int R = o.panel_rows ? o.panel_rows : default_panel_rows(bh);
   float split_frac = o.split_frac;
   if (o.panel_rows == 0) {
     // a configuration the autotuner measured for matrices like this one
@@ -118,10 +117,11 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     return fail(SMAT_ERR_UNSUPPORTED, "unsupported panel_rows for this block height");
   }
   h->R = R;
-  // class 0 serves the FP16, BF16 and FP8 forms (and the handle's info);
-  // class 1 the split form
+  // class 0 serves the FP16 and BF16 forms (and the handle's info), class 1
+  // the split form, class 2 the FP8 form
   for (int cls = 0; cls < kPlanClasses; cls++) {
     if (cls == 1 && !(forms & (1u << SMAT_FORM_SPLIT_BF16))) continue;
+    if (cls == 2 && !(forms & (1u << SMAT_FORM_FP8))) continue;
     st = build_plan(h->host, R, cls, h->pc[cls].plan);
     if (st != SMAT_OK) {
       delete h;
@@ -142,7 +142,6 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   } while (0)
 
   const HostBcsr& b = h->host;
-  SMAT_TRY(upload(&h->d_row_map, b.row_map.data(), b.row_map.size()));
   if (!b.kperm.empty()) SMAT_TRY(upload(&h->d_kperm, b.kperm.data(), b.kperm.size()));
   {
     int zero = 0;
@@ -154,9 +153,10 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     if (!pd.built) continue;
     SMAT_TRY(upload(&pd.d_stages, pd.plan.stages.data(), pd.plan.stages.size()));
     SMAT_TRY(upload(&pd.d_panels, pd.plan.panels.data(), pd.plan.panels.size()));
+    SMAT_TRY(upload(&pd.d_row_map, pd.plan.row_map.data(), pd.plan.row_map.size()));
     // work items per launch shape (NSUB 1 and 2): heavy panels split into
     // parts so that no CTA gets much more than the average
-    const int kind = cls == 1 ? TC_KIND_SPLIT : TC_KIND_PLAIN;
+    const int kind = cls == 1 ? TC_KIND_SPLIT : (cls == 2 ? TC_KIND_FP8 : TC_KIND_PLAIN);
     for (int nsub = 1; nsub <= 2; nsub++) {
       if (!tc_variant_supported(bh, R, nsub, kind)) continue;
       const int per_sm = tc_ctas_per_sm(bh, R, nsub, kind);
@@ -229,7 +229,7 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
       return fail(SMAT_ERR_UNSUPPORTED, "FP8 form: 16 x 16 blocks only");
     }
     SMAT_TRY(quantize_fp8(b, h->fp8_q, h->fp8_scale));
-    const Plan& pl = h->pc[0].plan;
+    const Plan& pl = h->pc[2].plan;
     const int64_t nst = (int64_t)pl.stages.size();
     // per stage: [nblk e4m3 blocks][nblk FP32 scales, padded][header]
     lay.assign(std::max<size_t>((size_t)nnzb * 256 + pl.headers.size() +
@@ -479,14 +479,14 @@ void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64
   P.aval = A->d_aval[form];
   P.panels = A->pc[plan_class(form)].d_panels;
   P.stages = A->pc[plan_class(form)].d_stages;
-  P.row_map = A->d_row_map;
+  P.row_map = A->pc[plan_class(form)].d_row_map;
   P.C = C;
   P.ldc = ldc;
   P.counters = reinterpret_cast<int32_t*>(ws + wl.counters);
   P.slabs = reinterpret_cast<float*>(ws + wl.slabs);
   P.N = (int32_t)N;
   P.n_tiles = (int32_t)((N + bn - 1) / bn);
-  P.nbr = (int32_t)A->host.nbr();
+  P.nbr = A->pc[plan_class(form)].plan.n_panels * A->pc[plan_class(form)].plan.R;  // plan rows (slots)
   P.c_f16 = c_dtype == SMAT_F16;
   // instruction descriptor (kind::f16): FP32 accumulator, FP16 (0) or BF16 (1)
   // operands, both K-major, M = 128; the kernel adds N per MMA group

@@ -309,14 +309,106 @@ smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
   if (R < 1 || R > 32) return fail(SMAT_ERR_INVALID, "panel rows must be in [1, 32]");
   const int64_t nbr = b.nbr();
   plan.R = R;
-  plan.n_panels = (int32_t)((nbr + R - 1) / R);
-  const int32_t P = plan.n_panels;
   if (b.nnzb() >= ((int64_t)1 << 31) - 1) return fail(SMAT_ERR_UNSUPPORTED, "too many blocks");
   const int32_t SB = stage_rows(cls) / b.bh;                 // blocks per stage
   const int32_t ST = stage_tiles(cls);                       // B tiles per stage
   const int32_t max_len = std::min<int32_t>(16, kMaxGroupN / b.bh);
   // MMA-issuing warp owning a slot: kMmaWarps equal ranges of slots
   auto owner = [R](uint32_t slot) -> uint32_t { return (uint32_t)((slot * kMmaWarps) / (uint32_t)R); };
+
+  // ---- panels and TMEM slots. A slot accumulates some blocks of one
+  // block row. Each issuing warp owns a fixed range of slots; one thread
+  // issues at most one MMA every ~78 cycles while the tensor pipe takes ~39
+  // per narrow MMA, so a warp with more than its share of a stage's blocks
+  // sets the pace. A block row holding more than a quarter of the panel's
+  // blocks (a hub row) is therefore dealt over kMmaWarps parts, block k of the
+  // row to part k mod kMmaWarps (every stage, a window of block columns, then
+  // finds work for every warp), part w in warp w's range at the same position
+  // (the epilogue adds the parts, in warp order); the other rows take the free
+  // slots heaviest first, each in the warp with the fewest blocks so far. A
+  // panel takes up to R consecutive block rows, fewer when its cut rows need
+  // the room. A slot accumulates blocks k0, k0 + step, ... < k1.
+  struct SlotSrc {
+    int32_t br = -1, k0 = 0, k1 = 0, step = 1;
+  };
+  std::vector<SlotSrc> slots;
+  std::vector<uint32_t> ext_masks;
+  const int32_t per_warp = R / kMmaWarps;
+  const bool can_cut = R % kMmaWarps == 0;
+  auto wrow = [&b](int64_t br) { return (int64_t)(b.rowptr[br + 1] - b.rowptr[br]); };
+  auto is_hub = [](int64_t w, int64_t W) { return w >= kMinCutBlocks && kMmaWarps * w > W; };
+  int32_t order[32], first_free[kMmaWarps], end_free[kMmaWarps];
+  int64_t load[kMmaWarps];
+  for (int64_t pos = 0; pos < nbr;) {
+    int32_t n = (int32_t)std::min<int64_t>(R, nbr - pos), h = 0;
+    for (;; n--) {  // n = 1 always fits: a single cut row takes one position per warp
+      int64_t W = 0;
+      for (int32_t r = 0; r < n; r++) W += wrow(pos + r);
+      h = 0;
+      if (can_cut)
+        for (int32_t r = 0; r < n; r++) h += is_hub(wrow(pos + r), W) ? 1 : 0;
+      if (h <= per_warp && n + (kMmaWarps - 1) * h <= R) break;
+    }
+    int64_t W = 0;
+    for (int32_t r = 0; r < n; r++) W += wrow(pos + r);
+    const size_t p = ext_masks.size();
+    slots.resize((p + 1) * (size_t)R);
+    SlotSrc* S = &slots[p * (size_t)R];
+    uint32_t ext = 0;
+    for (int w = 0; w < kMmaWarps; w++) {
+      load[w] = 0;
+      first_free[w] = end_free[w] = -1;
+    }
+    for (int32_t sl = 0; sl < R; sl++) {
+      const uint32_t w = owner((uint32_t)sl);
+      if (first_free[w] < 0) first_free[w] = sl;
+      end_free[w] = sl + 1;
+    }
+    int32_t nlight = 0, j = 0;
+    for (int32_t r = 0; r < n; r++) {
+      const int64_t br = pos + r, w_r = wrow(br);
+      if (h > 0 && is_hub(w_r, W)) {
+        for (int w = 0; w < kMmaWarps; w++) {
+          const int32_t sl = w * per_warp + j;
+          S[sl].br = (int32_t)br;
+          S[sl].k0 = b.rowptr[br] + w;
+          S[sl].k1 = b.rowptr[br + 1];
+          S[sl].step = kMmaWarps;
+          load[w] += (w_r - w + kMmaWarps - 1) / kMmaWarps;
+          if (w > 0) ext |= 1u << sl;
+        }
+        j++;
+      } else {
+        order[nlight++] = r;
+      }
+    }
+    for (int w = 0; w < kMmaWarps; w++)
+      if (first_free[w] >= 0) first_free[w] += j;
+    std::stable_sort(order, order + nlight, [&](int32_t x, int32_t y) { return wrow(pos + x) > wrow(pos + y); });
+    for (int32_t i = 0; i < nlight; i++) {
+      const int64_t br = pos + order[i];
+      int best = -1;
+      for (int w = 0; w < kMmaWarps; w++)
+        if (first_free[w] >= 0 && first_free[w] < end_free[w] && (best < 0 || load[w] < load[best])) best = w;
+      const int32_t sl = first_free[best]++;
+      S[sl].br = (int32_t)br;
+      S[sl].k0 = b.rowptr[br];
+      S[sl].k1 = b.rowptr[br + 1];
+      load[best] += wrow(br);
+    }
+    ext_masks.push_back(ext);
+    pos += n;
+  }
+  plan.n_panels = (int32_t)ext_masks.size();
+  const int32_t P = plan.n_panels;
+  // C row of each plan row (panel * R + slot) * bh + i; parts after the first
+  // of a cut row have none (the epilogue adds them into the first)
+  plan.row_map.assign((size_t)P * R * b.bh, -1);
+  for (size_t q = 0; q < slots.size(); q++) {
+    const SlotSrc& src = slots[q];
+    if (src.br < 0 || ((ext_masks[q / R] >> (q % R)) & 1u)) continue;
+    for (int32_t i = 0; i < b.bh; i++) plan.row_map[q * b.bh + i] = b.row_map[(size_t)src.br * b.bh + i];
+  }
   struct Local {
     std::vector<StageRec> stages;
     std::vector<uint8_t> hdr;
@@ -333,13 +425,13 @@ smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
     for (int32_t p = 0; p < P; p++) {
       Local& L = loc[p];
       ent.clear();
-      const int64_t br0 = (int64_t)p * R, br1 = std::min<int64_t>(nbr, br0 + R);
+      const SlotSrc* S = &slots[(size_t)p * R];
       uint32_t mask = 0;
-      for (int64_t br = br0; br < br1; br++) {
-        if (b.rowptr[br + 1] > b.rowptr[br]) mask |= 1u << (br - br0);
-        for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++)
-          ent.push_back({(int64_t)b.colidx[k] * 32 + (br - br0), k});
+      for (int32_t sl = 0; sl < R; sl++) {
+        if (S[sl].k1 > S[sl].k0) mask |= 1u << sl;
+        for (int32_t k = S[sl].k0; k < S[sl].k1; k += S[sl].step) ent.push_back({(int64_t)b.colidx[k] * 32 + sl, k});
       }
+      L.info.ext_mask = ext_masks[p];
       std::sort(ent.begin(), ent.end());
       L.info.nblk = (int32_t)ent.size();
       L.info.slot_mask = mask;

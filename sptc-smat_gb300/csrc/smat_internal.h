@@ -74,6 +74,9 @@ struct Plan {
   std::vector<StageRec> stages;
   std::vector<int32_t> stream_blk;   // BCSR block index at each stream position
   std::vector<uint8_t> headers;      // stage headers, concatenated (StageRec::hdr_off)
+  // C row of each plan row: inside a panel the block rows take TMEM slots in
+  // an order that gives the MMA-issuing warps equal shares of the blocks
+  std::vector<int32_t> row_map;
   int64_t n_groups = 0;              // MMA instructions per pass over A
   int64_t n_tiles = 0;               // B tile loads per pass over A
 };
@@ -117,6 +120,7 @@ struct PlanDev {
   bool built = false;
   PanelInfo* d_panels = nullptr;
   StageRec* d_stages = nullptr;
+  int32_t* d_row_map = nullptr;
   Sched sched[3];  // by NSUB (1, 2)
 };
 
@@ -129,7 +133,6 @@ struct SmatBcsrBody {
   int use24 = 0;
   int64_t n_24 = 0;
   int num_sms = 0;
-  int32_t* d_row_map = nullptr;
   int32_t* d_kperm = nullptr;  // column permutation for the B gather (or null)
   // A stream per form (F16, BF16, -, SPLIT): per stage the pre-swizzled
   // blocks in consumption order (hi, then lo for the split form) and the
@@ -159,7 +162,13 @@ namespace smat {
 // Kernel kind of an arithmetic form, its plan class, and the N-tile width
 // (128 * nsub) used for N.
 int kind_of(int32_t form);
-inline int plan_class(int32_t form) { return form == SMAT_FORM_SPLIT_BF16 ? 1 : 0; }
+inline int plan_class(int32_t form) {
+  return form == SMAT_FORM_SPLIT_BF16 ? 1 : (form == SMAT_FORM_FP8 ? 2 : 0);
+}
+inline int plan_class_of_kind(int kind) { return kind == TC_KIND_SPLIT ? 1 : (kind == TC_KIND_FP8 ? 2 : 0); }
+// Block rows per panel when the caller leaves it to the library: 128 rows
+// (8 blocks of 16 rows, 4 of 32), two TMEM accumulator buffers of 128 columns.
+inline int default_panel_rows(int bh) { return bh == 16 ? 8 : 4; }
 int pick_nsub(const smat_bcsr* h, int64_t N, int kind);
 
 // Workspace layout of one SpMM: [packed B (x2 for the split form)]

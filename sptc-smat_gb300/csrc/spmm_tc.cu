@@ -75,7 +75,7 @@ template <int BH, int R, int NSUB, int KIND>
 struct Cfg {
   static constexpr int BN = 128 * NSUB;                   // C columns per tile
   static constexpr int NOPS = (KIND == KIND_SPLIT) ? 2 : 1;
-  static constexpr int CLS = KIND == KIND_SPLIT ? 1 : 0;  // plan class (stage shape)
+  static constexpr int CLS = KIND == KIND_SPLIT ? 1 : (KIND == KIND_FP8 ? 2 : 0);  // plan class (stage shape)
   static constexpr int SB = stage_rows(CLS) / BH;         // A blocks per stage (at most)
   static constexpr int ST = stage_tiles(CLS);             // B tiles per stage (at most)
   static constexpr int HDRMAX = stage_hdr_max(SB);
@@ -102,14 +102,14 @@ struct Cfg {
   static constexpr int NPROD = 8;                         // copy warps
   static constexpr int NCONV = FP8 ? 4 : 0;               // FP8 converter warps (16..19)
   static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? NS : 0));
-  static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 16;
+  static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 16 + 4 * NS;
   static constexpr int THREADS = 512 + 32 * NCONV;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
   static_assert(R <= 32, "slot field is 5 bits");
   static_assert(SB <= kMaxStageBlocks, "position field is 5 bits");
-  static_assert(ST <= 2 * NPROD && ST <= kMaxStageTiles, "a copy warp issues at most two copies per stage");
+  static_assert(ST + 1 <= 2 * NPROD && ST <= kMaxStageTiles, "1 + ST copies per stage, at most two per copy warp");
   static_assert(NS_FIT >= 2, "two stages must fit");
   static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
   static_assert(!FP8 || (BH == 16 && NSUB == 1), "FP8 form: 16 x 16 blocks, 128-column tiles");
@@ -131,6 +131,11 @@ __device__ __noinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity, int*
 __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
                                            int where) {
   return mbar_try_wait(bar, parity) || mbar_wait(bar, parity, abort, err, where);
+}
+
+__device__ __forceinline__ bool wait_phase_sleepy(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
+                                                  int where) {
+  return mbar_try_wait(bar, parity) || mbar_wait_sleepy(bar, parity, abort, err, where);
 }
 
 __device__ __forceinline__ int shfl_i(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
@@ -158,6 +163,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   uint64_t* conv = drainbar + C::NMMA;  // FP8: the stage's A blocks are converted
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(conv + (C::FP8 ? C::NS : 0));
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* stage_ok = abort_flag + 1;  // [NS]: the copy leader's verdict on the stage's slot
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -319,14 +325,17 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
             const int tot = shfl_i(total, i);
             const int hw = shfl_i(hword, i);
             const int j = (int)(((uint32_t)pw - ci) & 7u);
+            const uint32_t s = ci % C::NS;
+            // The warp with copy 0 waits for the slot and passes its verdict
+            // to the other copy warps through a named barrier (blocked warps
+            // take no issue slots); so all copy warps move stage by stage and
+            // none can run a ring ahead and overwrite a stage still in use.
+            if (j == 0 && lane == 0)
+              stage_ok[s] = wait_phase(smem_u32(&empty[s]), ((ci / C::NS) & 1) ^ 1, abort_flag, err, ERR_PROD_A) ? 1 : 0;
+            named_bar_sync(1, 32 * C::NPROD);
             int good = 1;
             if (lane == 0) {
-              const uint32_t s = ci % C::NS;
-              // Every copy warp waits for every stage, with or without a copy
-              // in it: a parity wait only tells the last two phases apart, so
-              // a warp that skipped a stage could otherwise run a whole ring
-              // ahead and overwrite a stage still in use.
-              if (wait_phase(smem_u32(&empty[s]), ((ci / C::NS) & 1) ^ 1, abort_flag, err, ERR_PROD_A)) {
+              if (stage_ok[s]) {
                 const uint32_t st = smem0 + s * C::STAGE;
                 const uint32_t fb = smem_u32(&full[s]);
                 if (b1 == 0) {
@@ -454,6 +463,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       mbar_arrive(smem_u32(&accempty[1]));
     }
     constexpr int SLAB = R * BH * C::BN;  // floats per slab
+    constexpr int PW = (R % kMmaWarps == 0) ? R / kMmaWarps : 0;  // slots per issuing warp
     uint32_t k = 0;
     bool ok = true;
     for (int it = it0; it < it1 && ok; ++it) {
@@ -463,9 +473,12 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       const int panel = wi.panel;
       const bool split = wi.split >= 0;
       const uint32_t slot_mask = P.panels[panel].slot_mask;
+      // a hub row cut over the issuing warps has its parts in slots s, s + PW,
+      // s + 2 PW, ...; the parts after the first are added into it here
+      const uint32_t ext_mask = P.panels[panel].ext_mask;
       for (int nt = 0; nt < n_tiles; ++nt, ++k) {
         const uint32_t buf = k & 1;
-        if (!wait_phase(smem_u32(&accfull[buf]), (k >> 1) & 1, abort_flag, err, ERR_EPI)) {
+        if (!wait_phase_sleepy(smem_u32(&accfull[buf]), (k >> 1) & 1, abort_flag, err, ERR_EPI)) {
           ok = false;
           break;
         }
@@ -476,6 +489,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
           if (rb >= P.nbr) break;
+          if ((ext_mask >> s) & 1u) continue;
           const bool empty_slot = ((slot_mask >> s) & 1u) == 0;
           const int myrow = (!split && lane < BH) ? P.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
@@ -492,6 +506,17 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               } else {
 #pragma unroll
                 for (int m = 0; m < 16; ++m) v[m] = 0.0f;
+              }
+              if constexpr (PW > 0) {
+                for (int t = s + PW; t < R && ((ext_mask >> t) & 1u); t += PW) {
+                  if (((slot_mask >> t) & 1u) == 0) continue;
+                  float u[16];
+                  const uint32_t tb = dbase + j * C::SUB_COLS + t * BH + h;
+                  tmem_ld_x16(tb, u);
+                  tmem_st_x16_zero(tb);
+#pragma unroll
+                  for (int m = 0; m < 16; ++m) v[m] += u[m];
+                }
               }
               if (split) {
 #pragma unroll
@@ -533,6 +558,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
           if (rb >= P.nbr) break;
+          if ((ext_mask >> s) & 1u) continue;  // added into its first part's slab rows
           const int myrow = lane < BH ? P.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
@@ -632,11 +658,8 @@ static int ctas_per_sm_one() {
   X(16, 4, 1, 0)            \
   X(16, 8, 1, 0)            \
   X(16, 16, 1, 0)           \
-  X(16, 4, 2, 0)            \
-  X(16, 8, 2, 0)            \
   X(32, 4, 1, 0)            \
   X(32, 8, 1, 0)            \
-  X(32, 4, 2, 0)            \
   X(16, 4, 1, 1)            \
   X(16, 8, 1, 1)            \
   X(16, 16, 1, 1)           \

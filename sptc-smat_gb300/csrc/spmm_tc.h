@@ -11,17 +11,21 @@ namespace smat {
 
 // A pipeline STAGE carries up to stage_rows(cls) / bh A blocks of one panel
 // (in the order the kernel consumes them), up to stage_tiles(cls) packed B
-// tiles those blocks need, and the stage's MMA list. There are two stage
-// shapes ("plan classes"): class 0 for the FP16, BF16 and FP8 forms (24
-// blocks of 16 rows and 12 B tiles: 12 KB of A and 48 KB of B, three stages
-// in flight), class 1 for the split form, whose stages hold hi and lo
-// copies of everything (12 blocks and 6 tiles: the same bytes).
-constexpr int kPlanClasses = 2;
+// tiles those blocks need, and the stage's MMA list. There are three stage
+// shapes ("plan classes"), each the largest that still leaves three stages
+// in flight in shared memory: class 0 for the FP16 and BF16 forms (28
+// blocks of 16 rows and 14 B tiles: 14 KB of A and 56 KB of B), class 1
+// for the split form, whose stages hold hi and lo copies of everything (14
+// blocks and 7 tiles: the same bytes), class 2 for the FP8 form, whose
+// stages also stage the e4m3 blocks before conversion (24 blocks, 12
+// tiles).
+constexpr int kPlanClasses = 3;
 constexpr int kMaxStageTiles = 16;   // StageRec::kb capacity (a copy warp issues at most two copies)
 constexpr int kMaxStageBlocks = 31;  // the entry's position field has 5 bits
-__host__ __device__ constexpr int stage_rows(int cls) { return cls == 0 ? 384 : 192; }
-__host__ __device__ constexpr int stage_tiles(int cls) { return cls == 0 ? 12 : 6; }
-constexpr int kMmaWarps = 4;      // MMA-issuing warps; each owns a quarter of the panel's block rows
+__host__ __device__ constexpr int stage_rows(int cls) { return cls == 0 ? 448 : (cls == 1 ? 224 : 384); }
+__host__ __device__ constexpr int stage_tiles(int cls) { return cls == 0 ? 14 : (cls == 1 ? 7 : 12); }
+constexpr int kMmaWarps = 4;      // MMA-issuing warps; each owns a quarter of a panel's TMEM slots
+constexpr int kMinCutBlocks = 16; // a block row is cut over the issuing warps only from this many blocks
 constexpr int kMaxGroupN = 256;   // widest tcgen05.mma N (kind::f16, M = 128)
 
 // Per-panel record (8 x int32).
@@ -30,8 +34,9 @@ struct PanelInfo {
   int32_t nstages;     // stages of the panel
   int32_t nblk;        // blocks in the panel
   int32_t nucol;       // distinct block columns of the panel
-  uint32_t slot_mask;  // bit s set: block row s of the panel has at least one block
-  int32_t pad0, pad1, pad2;
+  uint32_t slot_mask;  // bit s set: slot s of the panel has at least one block
+  uint32_t ext_mask;   // bit s set: slot s holds a later part of the row in slot s - R / kMmaWarps
+  int32_t pad1, pad2;
 };
 
 // Per-stage record (96 bytes), read by the copy warps. In the device A
@@ -96,14 +101,14 @@ struct ProblemDesc {
   const uint8_t* aval;       // A stream of the form (see StageRec)
   const PanelInfo* panels;
   const StageRec* stages;
-  const int32_t* row_map;    // [rows_padded] BCSR row -> C row, or -1
+  const int32_t* row_map;    // [panels * R * bh] plan row -> C row, or -1
   void* C;
   int64_t ldc;
   float* slabs;              // partial sums of split panels: [slab][R * bh rows][BN] FP32
   int32_t* counters;         // [split panels][column tiles][4], zero before the launch
   int32_t N;
   int32_t n_tiles;
-  int32_t nbr;
+  int32_t nbr;               // plan block rows: panels * R (TMEM slots)
   int32_t c_f16;
   uint32_t idesc;            // instruction descriptor without the N field
   int32_t pad[3];

@@ -67,6 +67,33 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile i
   }
 }
 
+// mbar_wait for waits expected to be long (a whole panel): after a few
+// polls the thread sleeps between them so that it leaves the issue slots of
+// its SM sub-partition to the warps on the critical path.
+__device__ __noinline__ bool mbar_wait_sleepy(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
+                                              int where) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 4) __nanosleep(256);
+    if ((it & 7u) == 0) {
+      if (*abort) return false;
+      if (globaltimer() - t0 > kWaitTimeoutNs) {
+        *abort = 1;
+        atomicCAS(err, 0, where);
+        return false;
+      }
+    }
+  }
+}
+
+// Named barrier `id` over `nthreads` threads (whole warps); also orders the
+// participants' shared-memory accesses.
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // 2-D tiled TMA load into this CTA's shared memory, completing on `bar`.
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int32_t x,
                                             int32_t y, uint32_t bar) {

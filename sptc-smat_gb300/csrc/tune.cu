@@ -91,7 +91,7 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
     out->cached = 1;
     return SMAT_OK;
   }
-  const std::vector<int> Rs = bh == 16 ? std::vector<int>{8, 16} : std::vector<int>{4, 8};
+  const std::vector<int> Rs = bh == 16 ? std::vector<int>{4, 8, 16} : std::vector<int>{4, 8};
   const std::vector<float> fracs = {-1.0f, 2.0f, 1.0f, 0.5f};
   int prev = -1;
   cudaGetDevice(&prev);
@@ -149,7 +149,7 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
         break;
       }
       const double t = ms / kReps;
-      if (R == Rs.back() && f == 1.0f) ms_default = t;
+      if (R == default_panel_rows(bh) && f == 1.0f) ms_default = t;
       if (t < best.ms) {
         best.ms = t;
         best.panel_rows = R;

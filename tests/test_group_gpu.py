@@ -107,7 +107,7 @@ def test_autotune_picks_the_fastest_and_is_used(dev, smat_mod):
     smat_mod.lib().smat_autotune_clear()
     A = G.rmat(13, 120000, seed=4)
     r = smat_mod.autotune(A, form=smat_mod.FORM_F16, N=128)
-    assert not r["cached"] and r["panel_rows"] in (8, 16) and r["ms"] > 0
+    assert not r["cached"] and r["panel_rows"] in (4, 8, 16) and r["ms"] > 0
     assert r["ms"] <= r["ms_default"] * 1.0001            # the default shape is one of the candidates
     again = smat_mod.autotune(A, form=smat_mod.FORM_F16, N=128)
     assert again["cached"] and again["panel_rows"] == r["panel_rows"]

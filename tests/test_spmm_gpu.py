@@ -330,3 +330,37 @@ def test_column_permutation_keeps_the_product(dev, smat_mod, oracle_lib):
     rp, ci, v = smat_mod.csr_to_bcsr_host(Aq)
     erp, eci, ev, _ = M.export()
     assert np.array_equal(rp, erp) and np.array_equal(ci, eci) and np.array_equal(v.view(np.uint16), ev.view(np.uint16))
+
+
+def hub_matrix(rows, cols, seed):
+    """Mostly sparse rows with a few dense hub rows (every 97th and 211th row):
+    the planner cuts each hub block row over the four MMA-issuing warps and the
+    epilogue adds the parts."""
+    from smat import Csr
+    rng = np.random.default_rng(seed)
+    rp, ci = [0], []
+    for r in range(rows):
+        d = 0.6 if (r % 97 == 5 or r % 211 == 17) else 0.004
+        c = np.flatnonzero(rng.random(cols) < d).astype(np.int32)
+        ci.append(c)
+        rp.append(rp[-1] + len(c))
+    ci = np.concatenate(ci)
+    vals = rng.uniform(-1, 1, len(ci)).astype(np.float16).astype(np.float32)
+    return Csr(rows, cols, np.array(rp, np.int64), ci, vals)
+
+
+@pytest.mark.parametrize("R,split_frac,N", [(16, 0.0, 128), (8, 0.0, 128), (16, 0.05, 128), (16, 0.0, 256),
+                                            (16, 0.05, 256)])
+def test_hub_rows_cut_over_warps(dev, smat_mod, oracle_lib, R, split_frac, N):
+    A = hub_matrix(3000, 5000, seed=R + N)
+    Bh = np.random.default_rng(5).uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    ref = fp64_product(oracle_lib, A, Bh)
+    forms = (smat_mod.FORM_F16, smat_mod.FORM_BF16, smat_mod.FORM_SPLIT_BF16)
+    M = smat_mod.Bcsr(A, panel_rows=R, split_frac=split_frac, forms=forms)
+    B = torch.from_numpy(Bh).to(dev)
+    c1 = spmm(M, B, smat_mod.FORM_F16)
+    assert rel_err(c1, ref) <= 1e-3
+    assert np.array_equal(c1, spmm(M, B, smat_mod.FORM_F16))   # parts are added in a fixed order
+    assert rel_err(spmm(M, B, smat_mod.FORM_BF16), ref) <= 1e-2
+    assert rel_err(spmm(M, B.float(), smat_mod.FORM_SPLIT_BF16), ref) <= 1e-4
+    assert rel_err(spmm(M, B, smat_mod.FORM_F16, out_dtype=torch.float16), ref) <= 1e-3
