@@ -236,7 +236,9 @@ smat_status smat_spmm(const smat_bcsr* A, int32_t form, const void* B, int32_t b
 /* The two halves of smat_spmm, for callers that reuse one B with several
  * matrices or want to time the contraction alone: smat_spmm_pack_b writes B
  * into `workspace` in the tensor-core tile layout (4 KB tiles of 16 rows x
- * 128 columns, 32-byte swizzled; 8 KB hi+lo pairs for the split form);
+ * 128 columns, 32-byte swizzled, ordered [column tile][k-block] so that the
+ * tiles of consecutive k-blocks are contiguous; 8 KB hi+lo pairs for the
+ * split form);
  * smat_spmm_packed runs the contraction from that packed copy. */
 smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
                              int32_t b_layout, int64_t ldb, int64_t N, void* workspace,

@@ -475,7 +475,7 @@ void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64
   uint8_t* ws = const_cast<uint8_t*>(static_cast<const uint8_t*>(ws_));
   const int64_t bn = 128 * nsub;
   P.bpack = ws;
-  P.bp_ntiles = packed_b_tiles(N);
+  P.bp_kbs = (A->host.cols + 15) / 16;
   P.aval = A->d_aval[form];
   P.panels = A->pc[plan_class(form)].d_panels;
   P.stages = A->pc[plan_class(form)].d_stages;

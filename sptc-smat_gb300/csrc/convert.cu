@@ -98,7 +98,7 @@ __device__ __forceinline__ void pack_tile(const T* __restrict__ in, int layout, 
       if (OUT == OUT_SPLIT) l[i] = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(b)));
     }
   }
-  const int64_t tile = kb * ntiles + t;
+  const int64_t tile = (int64_t)t * ((K + 15) / 16) + kb;  // [column tile][k-block]
   const int sw = (r >> 2) & 1;
   constexpr int64_t kTileBytes = OUT == OUT_SPLIT ? 8192 : 4096;
   uint4* dst = reinterpret_cast<uint4*>(out + tile * kTileBytes + r * 32);

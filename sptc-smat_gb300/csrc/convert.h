@@ -15,7 +15,8 @@ int64_t packed_b_tiles(int64_t N);
 // Bytes of one packed copy of a K x N operand.
 size_t packed_b_bytes(int64_t K, int64_t N);
 
-// Packs B into 4 KB swizzled tiles ordered [k-block][128-column tile].
+// Packs B into 4 KB swizzled tiles ordered [128-column tile][k-block], so
+// that the tiles of consecutive k-blocks of one column tile are contiguous.
 // in_dtype: 0 F32, 1 F16, 2 BF16; layout: 0 row-major (k*ldi + n), 1
 // column-major (k + n*ldi); out_mode: 0 FP16, 1 BF16, 2 hi+lo BF16 (8 KB
 // [hi | lo] per tile, twice packed_b_bytes).

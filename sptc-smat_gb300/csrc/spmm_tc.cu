@@ -107,6 +107,7 @@ struct Cfg {
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
+  static_assert(NSUB == 1, "packed B is [column tile][k-block]: a stage tile is one 128-column tile");
   static_assert(R <= 32, "slot field is 5 bits");
   static_assert(SB <= kMaxStageBlocks, "position field is 5 bits");
   static_assert(ST + 1 <= 2 * NPROD && ST <= kMaxStageTiles, "1 + ST copies per stage, at most two per copy warp");
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
           const uint32_t my_ci = ci + (uint32_t)lane;
           const int j0 = (int)(((uint32_t)pw - my_ci) & 7u);
           int64_t off1 = 0, off2 = 0, pf_off = 0;
-          int bytes1 = 0, total = 0, hword = 0, has2 = 0, pf_bytes = 0;
+          int bytes1 = 0, bytes2 = 0, dst1 = 0, dst2 = 0, total = 0, hword = 0, pf_bytes = 0;
           if (lane < cnt) {
             const StageRec* rp = P.stages + stage0 + base + lane;
             const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
@@ -295,13 +296,19 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               off1 = pf_off;
               bytes1 = pf_bytes;
               total = bytes1 + ntl * (int)C::TILEB;
-            } else if (j0 <= ntl) {
-              off1 = ((int64_t)rp->kb[j0 - 1] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
-              bytes1 = (int)C::TILEB;
             }
-            if (j0 + 8 <= ntl) {  // the warp's second copy: tile j0 + 7
-              has2 = 1;
-              off2 = ((int64_t)rp->kb[j0 + 7] * P.bp_ntiles + bcol) * (4096 * C::NOPS);
+            // B copies, one per tile (several copies in flight land sooner
+            // than one long copy of adjacent tiles): copy j >= 1 brings tile
+            // j - 1, this warp's are tiles j0 - 1 and j0 + 7
+            if (j0 >= 1 && j0 <= ntl) {
+              off1 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 - 1]) * (4096 * C::NOPS);
+              bytes1 = (int)C::TILEB;
+              dst1 = j0 - 1;
+            }
+            if (j0 + 8 <= ntl) {
+              off2 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 + 7]) * (4096 * C::NOPS);
+              bytes2 = (int)C::TILEB;
+              dst2 = j0 + 7;
             }
           }
           // A comes from HBM: prefetch each stage's A region into L2 kPrefetchAhead
@@ -319,7 +326,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               if (lane == 0 && (int)(((uint32_t)pw - ci) & 7u) == 0) bulk_prefetch_l2(P.aval + po, (uint32_t)pb);
             }
             const int b1 = shfl_i(bytes1, i);
-            const int h2 = shfl_i(has2, i);
+            const int b2 = shfl_i(bytes2, i);
+            const int d1 = shfl_i(dst1, i);
+            const int d2 = shfl_i(dst2, i);
             const int64_t o1 = shfl_l(off1, i);
             const int64_t o2 = shfl_l(off2, i);
             const int tot = shfl_i(total, i);
@@ -345,10 +354,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
                   mbar_arrive_expect_tx(fb, (uint32_t)tot);
                   bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), P.aval + o1, (uint32_t)b1, fb, pol_a);
                 } else {
-                  bulk_load_hint(st + C::OFF_B + (j - 1) * C::TILEB, P.bpack + o1, C::TILEB, fb, pol_b);
+                  bulk_load_hint(st + C::OFF_B + d1 * C::TILEB, P.bpack + o1, (uint32_t)b1, fb, pol_b);
                 }
-                if (h2) bulk_load_hint(st + C::OFF_B + (j + 7) * C::TILEB, P.bpack + o2, C::TILEB, fb, pol_b);
-                if (b1 != 0) last_mine = ci;
+                if (b2 != 0) bulk_load_hint(st + C::OFF_B + d2 * C::TILEB, P.bpack + o2, (uint32_t)b2, fb, pol_b);
+                if (b1 != 0 || b2 != 0) last_mine = ci;
               } else {
                 good = 0;
               }
@@ -597,6 +606,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     }
   }
 
+  // lane 0 of the MMA and copy warps ran their roles alone: reconverge
+  // every warp before the CTA-wide barrier
+  __syncwarp();
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {

@@ -97,7 +97,7 @@ struct WorkItem {
 struct ProblemDesc {
   const uint8_t* bpack;      // B in 4 KB tiles [k-block][128-column tile] (pack_b); the split
                              // form stores [hi tile | lo tile] pairs, 8 KB per tile
-  int64_t bp_ntiles;         // 128-column tiles per k-block in bpack
+  int64_t bp_kbs;            // k-blocks per 128-column tile in bpack ([column tile][k-block])
   const uint8_t* aval;       // A stream of the form (see StageRec)
   const PanelInfo* panels;
   const StageRec* stages;

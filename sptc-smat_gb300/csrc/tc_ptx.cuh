@@ -89,9 +89,12 @@ __device__ __noinline__ bool mbar_wait_sleepy(uint32_t bar, uint32_t parity, vol
 }
 
 // Named barrier `id` over `nthreads` threads (whole warps); also orders the
-// participants' shared-memory accesses.
+// participants' shared-memory accesses. The warp reconverges first and the
+// barrier is the non-aligned form, which counts every thread's own arrival,
+// so a lane still busy (say, waiting on an mbarrier) holds the barrier.
 __device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t nthreads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+  __syncwarp();
+  asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 // 2-D tiled TMA load into this CTA's shared memory, completing on `bar`.
