@@ -71,8 +71,8 @@ static void free_handle(smat_bcsr* h) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (PlanDev& pd : h->pc) {
-    void* pp[] = {pd.d_stages, pd.d_panels, pd.d_row_map, pd.sched[1].d_cta_ptr, pd.sched[1].d_cta_items, pd.sched[1].d_items,
-                  pd.sched[2].d_cta_ptr, pd.sched[2].d_cta_items, pd.sched[2].d_items};
+    void* pp[] = {pd.d_stages, pd.d_panels, pd.d_row_map, pd.sched[1].d_order, pd.sched[1].d_items,
+                  pd.sched[2].d_order, pd.sched[2].d_items};
     for (void* p : pp)
       if (p) cudaFree(p);
   }
@@ -162,14 +162,13 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
       const int per_sm = tc_ctas_per_sm(bh, R, nsub, kind);
       const int workers = std::max(1, h->num_sms * per_sm);
       std::vector<WorkItem> items;
-      std::vector<int32_t> cta_ptr, cta_items;
+      std::vector<int32_t> order;
       Sched& sc = pd.sched[nsub];
-      build_work_items(pd.plan, bh, workers, frac, items, cta_ptr, cta_items, sc.n_split, sc.n_slabs);
+      build_work_items(pd.plan, bh, workers, frac, items, order, sc.n_split, sc.n_slabs);
       sc.grid = std::max(1, std::min<int>(workers, (int)items.size()));
-      cta_ptr.resize(sc.grid + 1);  // queues past the item count are empty
+      sc.n_items = (int32_t)items.size();
       SMAT_TRY(upload(&sc.d_items, items.data(), items.size()));
-      SMAT_TRY(upload(&sc.d_cta_ptr, cta_ptr.data(), cta_ptr.size()));
-      SMAT_TRY(upload(&sc.d_cta_items, cta_items.data(), cta_items.size()));
+      SMAT_TRY(upload(&sc.d_order, order.data(), order.size()));
     }
   }
 
@@ -461,7 +460,7 @@ WsLayout smat::ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
   const int nsub = pick_nsub(A, N, kind_of(form));
   const Sched& sc = A->pc[plan_class(form)].sched[nsub];
   const int64_t bn = 128 * nsub, n_tiles = (std::max<int64_t>(N, 1) + bn - 1) / bn;
-  w.counter_bytes = ((size_t)sc.n_split * n_tiles * 4 * sizeof(int32_t) + 255) / 256 * 256;
+  w.counter_bytes = (16 + (size_t)sc.n_split * n_tiles * 4 * sizeof(int32_t) + 255) / 256 * 256;
   w.slabs = w.counters + w.counter_bytes;
   w.total = w.slabs + (size_t)sc.n_slabs * n_tiles * A->R * A->host.bh * bn * sizeof(float);
   return w;
@@ -482,7 +481,7 @@ void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64
   P.row_map = A->pc[plan_class(form)].d_row_map;
   P.C = C;
   P.ldc = ldc;
-  P.counters = reinterpret_cast<int32_t*>(ws + wl.counters);
+  P.counters = reinterpret_cast<int32_t*>(ws + wl.counters + 16);  // after the next-item counter
   P.slabs = reinterpret_cast<float*>(ws + wl.slabs);
   P.N = (int32_t)N;
   P.n_tiles = (int32_t)((N + bn - 1) / bn);
@@ -603,14 +602,17 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   std::memset(&args, 0, sizeof(args));
   const WsLayout wl = ws_layout(A, form, N);
   fill_problem(A, form, packed_b, N, C, c_dtype, ldc, nsub, wl, args.one);
-  args.cta_ptr = sc.d_cta_ptr;
-  args.cta_items = sc.d_cta_items;
+  args.order = sc.d_order;
+  args.n_items = sc.n_items;
   args.items = sc.d_items;
   args.err = A->d_err;
-  if (sc.n_split > 0) {
-    // the split panels' counters start at zero in every launch
-    cudaError_t e = cudaMemsetAsync(args.one.counters, 0, wl.counter_bytes, static_cast<cudaStream_t>(stream_));
-    if (e != cudaSuccess) return cuda_fail(e, "clearing the split-panel counters");
+  uint8_t* ctr = static_cast<uint8_t*>(const_cast<void*>(packed_b)) + wl.counters;
+  args.next_item = reinterpret_cast<int32_t*>(ctr);
+  {
+    // the next-item counter and the split panels' counters start at zero
+    // in every launch
+    cudaError_t e = cudaMemsetAsync(ctr, 0, wl.counter_bytes, static_cast<cudaStream_t>(stream_));
+    if (e != cudaSuccess) return cuda_fail(e, "clearing the work counters");
   }
   cudaError_t e = tc_launch(bh, R, nsub, kind, args, sc.grid, static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "spmm kernel launch");

@@ -549,9 +549,8 @@ smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
 }
 
 void build_work_items_multi(const std::vector<const Plan*>& plans, const std::vector<int32_t>& bhs, int32_t workers,
-                            double max_item_frac, std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
-                            std::vector<int32_t>& cta_items, std::vector<int32_t>& n_split,
-                            std::vector<int32_t>& n_slabs) {
+                            double max_item_frac, std::vector<WorkItem>& items, std::vector<int32_t>& order,
+                            std::vector<int32_t>& n_split, std::vector<int32_t>& n_slabs) {
   // cost of a stage in units of one A block: the block copies, the B tiles
   // (a 4 KB tile moves 8x the bytes of a block, from L2) and a fixed
   // per-stage hand-off cost; per item, the epilogue (R * bh rows of C)
@@ -623,45 +622,22 @@ void build_work_items_multi(const std::vector<const Plan*>& plans, const std::ve
       n_slabs[q] += part;
     }
   }
-  assign_items(icost, workers, cta_ptr, cta_items);
+  order_items(icost, order);
 }
 
 void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
-                      std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
-                      std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs) {
+                      std::vector<WorkItem>& items, std::vector<int32_t>& order, int32_t& n_split,
+                      int32_t& n_slabs) {
   std::vector<int32_t> ns, nl;
-  build_work_items_multi({&pl}, {bh}, workers, max_item_frac, items, cta_ptr, cta_items, ns, nl);
+  build_work_items_multi({&pl}, {bh}, workers, max_item_frac, items, order, ns, nl);
   n_split = ns[0];
   n_slabs = nl[0];
 }
 
-void assign_items(const std::vector<double>& cost, int32_t workers, std::vector<int32_t>& cta_ptr,
-                  std::vector<int32_t>& cta_items) {
-  const int32_t n = (int32_t)cost.size();
-  std::vector<int32_t> order(n);
+void order_items(const std::vector<double>& cost, std::vector<int32_t>& order) {
+  order.resize(cost.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
-  // min-heap of (load, worker)
-  std::vector<std::pair<double, int32_t>> heap;
-  for (int32_t w = 0; w < workers; w++) heap.push_back({0.0, w});
-  auto cmp = [](const std::pair<double, int32_t>& a, const std::pair<double, int32_t>& b) {
-    return a.first > b.first || (a.first == b.first && a.second > b.second);
-  };
-  std::make_heap(heap.begin(), heap.end(), cmp);
-  std::vector<std::vector<int32_t>> q(workers);
-  for (int32_t it : order) {
-    std::pop_heap(heap.begin(), heap.end(), cmp);
-    auto& w = heap.back();
-    q[w.second].push_back(it);
-    w.first += cost[it];
-    std::push_heap(heap.begin(), heap.end(), cmp);
-  }
-  cta_ptr.assign(workers + 1, 0);
-  cta_items.clear();
-  for (int32_t w = 0; w < workers; w++) {
-    cta_items.insert(cta_items.end(), q[w].begin(), q[w].end());
-    cta_ptr[w + 1] = (int32_t)cta_items.size();
-  }
 }
 
 }  // namespace smat

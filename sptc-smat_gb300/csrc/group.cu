@@ -30,8 +30,9 @@ struct Launch {
   int bh = 16, R = 16, nsub = 1, kind = 0, grid = 1;
   ProblemDesc* d_probs = nullptr;
   WorkItem* d_items = nullptr;
-  int32_t* d_cta_ptr = nullptr;
-  int32_t* d_cta_items = nullptr;
+  int32_t* d_order = nullptr;
+  int32_t n_items = 0;
+  int32_t ctr = 0;  // int offset of the launch's next-item counter in d_counters
 };
 
 }  // namespace
@@ -57,8 +58,7 @@ static void group_free(smat_group* g) {
   for (Launch& l : g->launches) {
     cudaFree(l.d_probs);
     cudaFree(l.d_items);
-    cudaFree(l.d_cta_ptr);
-    cudaFree(l.d_cta_items);
+    cudaFree(l.d_order);
   }
   cudaFree(g->d_ws);
   cudaFree(g->d_counters);
@@ -132,7 +132,7 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
   };
   std::vector<Scratch> sc(count);
   std::vector<std::vector<WorkItem>> v_items;
-  std::vector<std::vector<int32_t>> v_ptr, v_cta;
+  std::vector<std::vector<int32_t>> v_order;
   std::vector<std::vector<int32_t>> v_members;
   for (auto& kv : variants) {
     const auto& members = kv.second;
@@ -145,8 +145,8 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     }
     const int workers = std::max(1, g->num_sms * tc_ctas_per_sm(bh, std::get<1>(kv.first), nsub, kind));
     std::vector<WorkItem> items;
-    std::vector<int32_t> cta_ptr, cta_items, n_split, n_slabs;
-    build_work_items_multi(plans, bhs, workers, 1.0, items, cta_ptr, cta_items, n_split, n_slabs);
+    std::vector<int32_t> order, n_split, n_slabs;
+    build_work_items_multi(plans, bhs, workers, 1.0, items, order, n_split, n_slabs);
     for (size_t m = 0; m < members.size(); m++) {
       const smat_problem& p = probs[members[m]];
       const int64_t bn = 128 * nsub, n_tiles = (p.N + bn - 1) / bn;
@@ -162,15 +162,16 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     l.nsub = nsub;
     l.kind = kind;
     l.grid = std::max(1, std::min<int>(workers, (int)items.size()));
-    cta_ptr.resize(l.grid + 1);
+    l.n_items = (int32_t)items.size();
     g->launches.push_back(l);
     v_items.push_back(std::move(items));
-    v_ptr.push_back(std::move(cta_ptr));
-    v_cta.push_back(std::move(cta_items));
+    v_order.push_back(std::move(order));
     v_members.push_back(members);
   }
-  // one scratch allocation for all problems, one for all counters
-  size_t ws_total = 0, ctr_total = 0;
+  // one scratch allocation for all problems, one for all counters: each
+  // launch's next-item counter (16 bytes apart), then the split panels'
+  size_t ws_total = 0, ctr_total = 4 * g->launches.size();
+  for (size_t v = 0; v < g->launches.size(); v++) g->launches[v].ctr = (int32_t)(4 * v);
   for (Scratch& s : sc) {
     s.ws_off = ws_total;
     ws_total += (s.packed + s.slabs + 255) / 256 * 256;
@@ -217,8 +218,7 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     }
     GTRY(upload_vec(&l.d_probs, descs));
     GTRY(upload_vec(&l.d_items, v_items[v]));
-    GTRY(upload_vec(&l.d_cta_ptr, v_ptr[v]));
-    GTRY(upload_vec(&l.d_cta_items, v_cta[v]));
+    GTRY(upload_vec(&l.d_order, v_order[v]));
   }
 #undef GTRY
   *out = g;
@@ -243,8 +243,9 @@ smat_status smat_group_run(smat_group* g, void* stream_) {
     SpmmArgs args;
     std::memset(&args, 0, sizeof(args));
     args.probs = l.d_probs;
-    args.cta_ptr = l.d_cta_ptr;
-    args.cta_items = l.d_cta_items;
+    args.order = l.d_order;
+    args.n_items = l.n_items;
+    args.next_item = g->d_counters + l.ctr;
     args.items = l.d_items;
     args.err = g->d_err;
     e = tc_launch(l.bh, l.R, l.nsub, l.kind, args, l.grid, s);

@@ -95,20 +95,21 @@ smat_status quantize_fp8(const HostBcsr& b, std::vector<uint8_t>& q, std::vector
 
 // Work items of one launch shape: panels whose cost exceeds max_item_frac
 // of the per-worker average are split into parts (stage ranges) of about
-// that size; the items are then assigned to `workers` queues. n_split =
-// split panels, n_slabs = their parts (one partial-sum slab per part and
-// column tile).
+// that size. `order` lists the items by decreasing estimated cost: the CTAs
+// of a launch take them in that order, each the next one when it is done
+// with its last (the first from its own index). n_split = split panels,
+// n_slabs = their parts (one partial-sum slab per part and column tile).
 void build_work_items(const Plan& pl, int32_t bh, int32_t workers, double max_item_frac,
-                      std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
-                      std::vector<int32_t>& cta_items, int32_t& n_split, int32_t& n_slabs);
+                      std::vector<WorkItem>& items, std::vector<int32_t>& order, int32_t& n_split,
+                      int32_t& n_slabs);
 
 
 // ------------------------------------------------------------------ handle
 // Work list of one launch shape (NSUB).
 struct Sched {
   int grid = 0;
-  int32_t* d_cta_ptr = nullptr;
-  int32_t* d_cta_items = nullptr;
+  int32_t n_items = 0;
+  int32_t* d_order = nullptr;  // items by decreasing estimated cost
   WorkItem* d_items = nullptr;
   int32_t n_split = 0;  // panels split into parts
   int32_t n_slabs = 0;  // parts of split panels
@@ -172,6 +173,7 @@ inline int default_panel_rows(int bh) { return bh == 16 ? 8 : 4; }
 int pick_nsub(const smat_bcsr* h, int64_t N, int kind);
 
 // Workspace layout of one SpMM: [packed B (x2 for the split form)]
+// [the launch's next-item counter, 16 bytes]
 // [per split panel, column tile and TMEM lane quadrant: an int counter]
 // [per part of a split panel and column tile: an R*bh x BN FP32 slab].
 struct WsLayout {
@@ -188,9 +190,8 @@ void fill_problem(const smat_bcsr* A, int32_t form, const void* ws, int64_t N, v
 // split decisions use the total over all problems; n_split / n_slabs per
 // problem.
 void build_work_items_multi(const std::vector<const Plan*>& plans, const std::vector<int32_t>& bhs, int32_t workers,
-                            double max_item_frac, std::vector<WorkItem>& items, std::vector<int32_t>& cta_ptr,
-                            std::vector<int32_t>& cta_items, std::vector<int32_t>& n_split,
-                            std::vector<int32_t>& n_slabs);
+                            double max_item_frac, std::vector<WorkItem>& items, std::vector<int32_t>& order,
+                            std::vector<int32_t>& n_split, std::vector<int32_t>& n_slabs);
 
 // ------------------------------------------------------------------ autotuner
 // Key of the tuning cache: block-density statistics of a matrix (blocks per
@@ -215,8 +216,7 @@ bool tune_key_of(const HostBcsr& b, int kind, int64_t N, TuneKey& key);
 bool tune_lookup(const TuneKey& key, TuneVal& val);
 void tune_store(const TuneKey& key, const TuneVal& val);
 
-// Longest-processing-time assignment of items to `workers` queues.
-void assign_items(const std::vector<double>& item_cost, int32_t workers,
-                  std::vector<int32_t>& cta_ptr, std::vector<int32_t>& cta_items);
+// Item indices by decreasing cost (ties by index).
+void order_items(const std::vector<double>& item_cost, std::vector<int32_t>& order);
 
 }  // namespace smat

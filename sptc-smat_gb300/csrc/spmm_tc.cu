@@ -68,8 +68,16 @@ enum : int {
   ERR_MMA_B = 203,
   ERR_EPI = 301,
   ERR_CONV = 302,
-  ERR_DRAIN = 401
+  ERR_DRAIN = 401,
+  ERR_ITEM_TAKE = 103,  // the copy warps waited for a free item-ring slot
+  ERR_ITEM_MMA = 204,   // an MMA warp waited for its next item
+  ERR_ITEM_EPI = 303,
+  ERR_ITEM_CONV = 304
 };
+
+// Entries of the CTA's ring of work items (the copy warps take items from
+// the launch's counter and run up to a few items ahead of the other roles).
+constexpr int kItemRing = 4;
 
 template <int BH, int R, int NSUB, int KIND>
 struct Cfg {
@@ -101,8 +109,10 @@ struct Cfg {
   static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
   static constexpr int NPROD = 8;                         // copy warps
   static constexpr int NCONV = FP8 ? 4 : 0;               // FP8 converter warps (16..19)
-  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? NS : 0));
-  static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 16 + 4 * NS;
+  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? NS : 0) + 2 * kItemRing);
+  // then the TMEM address, the abort flag, stage_ok[NS], the item ring and
+  // the copy warps' current item
+  static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 8 + 4 * (NS + kItemRing + 1);
   static constexpr int THREADS = 512 + 32 * NCONV;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
@@ -139,6 +149,37 @@ __device__ __forceinline__ bool wait_phase_sleepy(uint32_t bar, uint32_t parity,
   return mbar_try_wait(bar, parity) || mbar_wait_sleepy(bar, parity, abort, err, where);
 }
 
+// Item k of the CTA from the item ring, for a role run by lane 0 alone:
+// waits for it, reads it and frees the ring slot. idx = -1: no more work.
+// Returns false when the CTA aborted.
+__device__ __forceinline__ bool take_item_lane0(uint64_t* itemfull, uint64_t* itemempty, const volatile int* ring,
+                                                uint32_t k, volatile int* abort, int* err, int where, int& idx) {
+  const uint32_t r = k % kItemRing;
+  if (!wait_phase(smem_u32(&itemfull[r]), (k / kItemRing) & 1, abort, err, where)) return false;
+  idx = ring[r];
+  mbar_arrive(smem_u32(&itemempty[r]));
+  return true;
+}
+
+// The same for a whole warp: lane 0 waits and reads, the warp gets the
+// index by shuffle (so the warp's decision is uniform).
+__device__ __forceinline__ bool take_item_warp(uint64_t* itemfull, uint64_t* itemempty, const volatile int* ring,
+                                               uint32_t k, int lane, volatile int* abort, int* err, int where,
+                                               int& idx) {
+  int got = 1, v = -1;
+  if (lane == 0) {
+    const uint32_t r = k % kItemRing;
+    got = wait_phase_sleepy(smem_u32(&itemfull[r]), (k / kItemRing) & 1, abort, err, where) ? 1 : 0;
+    if (got) {
+      v = ring[r];
+      mbar_arrive(smem_u32(&itemempty[r]));
+    }
+  }
+  got = __shfl_sync(0xffffffffu, got, 0);
+  idx = __shfl_sync(0xffffffffu, v, 0);
+  return got != 0;
+}
+
 __device__ __forceinline__ int shfl_i(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
   const int lo = __shfl_sync(0xffffffffu, (int)(uint32_t)(uint64_t)v, src);
@@ -162,9 +203,13 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   uint64_t* accempty = accfull + 2;
   uint64_t* drainbar = accempty + 2;
   uint64_t* conv = drainbar + C::NMMA;  // FP8: the stage's A blocks are converted
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(conv + (C::FP8 ? C::NS : 0));
+  uint64_t* itemfull = conv + (C::FP8 ? C::NS : 0);  // [kItemRing] an item index is in the ring
+  uint64_t* itemempty = itemfull + kItemRing;        // [kItemRing] every role has read it
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(itemempty + kItemRing);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   volatile int* stage_ok = abort_flag + 1;  // [NS]: the copy leader's verdict on the stage's slot
+  volatile int* item_ring = stage_ok + C::NS;     // [kItemRing] item indices (-1: no more work)
+  volatile int* cur_item = item_ring + kItemRing;  // the copy warps' current item
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -181,6 +226,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     for (int i = 0; i < C::NMMA; i++) mbar_init(smem_u32(&drainbar[i]), 1);
     if (C::FP8)
       for (int i = 0; i < C::NS; i++) mbar_init(smem_u32(&conv[i]), C::NCONV);
+    for (int i = 0; i < kItemRing; i++) {
+      mbar_init(smem_u32(&itemfull[i]), 1);
+      mbar_init(smem_u32(&itemempty[i]), C::NMMA + 4 + C::NCONV);  // lane 0 of every other warp
+    }
     *abort_flag = 0;
     fence_barrier_init();
   }
@@ -193,8 +242,6 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  const int it0 = args.cta_ptr[blockIdx.x];
-  const int it1 = args.cta_ptr[blockIdx.x + 1];
   int* err = args.err;
   const uint32_t smem0 = smem_u32(smem);
 
@@ -208,8 +255,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     const int ct = threadIdx.x - 512;
     uint32_t ci = 0;
     bool ok = true;
-    for (int it = it0; it < it1 && ok; ++it) {
-      const WorkItem wi = args.items[args.cta_items[it]];
+    for (uint32_t kk = 0; ok; ++kk) {
+      int idx = -1;
+      if (!take_item_warp(itemfull, itemempty, item_ring, kk, lane, abort_flag, err, ERR_ITEM_CONV, idx)) {
+        ok = false;
+        break;
+      }
+      if (idx < 0) break;
+      const WorkItem wi = args.items[idx];
       const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
       const int n_tiles = P.n_tiles;
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
@@ -263,8 +316,29 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     uint32_t ci = 0;
     bool ok = true;
     uint32_t last_mine = 0xffffffffu;  // last stage this warp copied into (for the drain)
-    for (int it = it0; it < it1 && ok; ++it) {
-      const WorkItem wi = args.items[args.cta_items[it]];
+    for (uint32_t kk = 0; ok; ++kk) {
+      // The CTA's next item: lane 0 of the first copy warp takes it from the
+      // launch's order (the CTA's own index first, then the shared
+      // counter), puts it in the item ring for the other roles once they
+      // have read the entry it replaces, and hands it to the copy warps.
+      if (pw == 0 && lane == 0) {
+        const uint32_t r = kk % kItemRing;
+        int idx = -2;  // -2: aborted
+        if (wait_phase(smem_u32(&itemempty[r]), ((kk / kItemRing) & 1) ^ 1, abort_flag, err, ERR_ITEM_TAKE)) {
+          const int pos = kk == 0 ? (int)blockIdx.x : (int)gridDim.x + atomicAdd(args.next_item, 1);
+          idx = pos < args.n_items ? args.order[pos] : -1;
+          item_ring[r] = idx;
+          mbar_arrive(smem_u32(&itemfull[r]));
+        }
+        *cur_item = idx;
+      }
+      named_bar_sync(1, 32 * C::NPROD);
+      const int idx = *cur_item;
+      if (idx < 0) {
+        ok = idx == -1;
+        break;
+      }
+      const WorkItem wi = args.items[idx];
       const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
       const int n_tiles = P.n_tiles;
       const int stage0 = P.panels[wi.panel].stage_off;
@@ -387,8 +461,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       // cycles; four keep the tensor pipe near its rate for these narrow MMAs.
       uint32_t ci = 0, k = 0, slot_s = 0, phase_s = 0;
       bool ok = true, issued = false;
-      for (int it = it0; it < it1 && ok; ++it) {
-        const WorkItem wi = args.items[args.cta_items[it]];
+      for (uint32_t kk = 0; ok; ++kk) {
+        int idx = -1;
+        if (!take_item_lane0(itemfull, itemempty, item_ring, kk, abort_flag, err, ERR_ITEM_MMA, idx)) {
+          ok = false;
+          break;
+        }
+        if (idx < 0) break;
+        const WorkItem wi = args.items[idx];
         const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
         const int n_tiles = P.n_tiles;
         const uint32_t idesc0 = P.idesc;  // without the N field
@@ -475,8 +555,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     constexpr int PW = (R % kMmaWarps == 0) ? R / kMmaWarps : 0;  // slots per issuing warp
     uint32_t k = 0;
     bool ok = true;
-    for (int it = it0; it < it1 && ok; ++it) {
-      const WorkItem wi = args.items[args.cta_items[it]];
+    for (uint32_t kk = 0; ok; ++kk) {
+      int idx = -1;
+      if (!take_item_warp(itemfull, itemempty, item_ring, kk, lane, abort_flag, err, ERR_ITEM_EPI, idx)) {
+        ok = false;
+        break;
+      }
+      if (idx < 0) break;
+      const WorkItem wi = args.items[idx];
       const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
       const int n_tiles = P.n_tiles;
       const int panel = wi.panel;

@@ -117,13 +117,19 @@ struct ProblemDesc {
 // Kernel arguments (one __grid_constant__ parameter). A single SpMM passes
 // its problem by value (one); a grouped launch passes a device array
 // (probs, indexed by WorkItem::prob).
+// A launch: its problems and work items. CTA b takes the items order[b],
+// then order[grid + atomicAdd(next_item, 1)], ... until the list is done:
+// the items are sorted by decreasing estimated cost, so whichever CTA is
+// free first takes the largest item left (the counter is zero at launch).
 struct SpmmArgs {
   ProblemDesc one;
   const ProblemDesc* probs;
-  const int32_t* cta_ptr;    // [grid + 1]
-  const int32_t* cta_items;  // work items, per CTA
+  const int32_t* order;      // [n_items] item indices by decreasing cost
+  int32_t* next_item;        // zero at launch
   const WorkItem* items;
   int* err;
+  int32_t n_items;
+  int32_t pad_;
 };
 
 // Kernel kinds: 0 plain (FP16 or BF16 A and B), 1 split hi+lo BF16, 2 FP8 A
