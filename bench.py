@@ -236,6 +236,48 @@ def run_reference(args):
         pg.barrier()
 
 
+REORDER_WORKLOAD = {
+    "workload": "rmat16_2M_reorder_tau0.6",
+    "generator": "R-MAT 2^16, a=0.57 b=c=0.19 d=0.05, 2.0M unique, rows permuted",
+    "reorder": "Keeper (-a 5), tau=0.6, col_block=16, row_block=16, fixed size (-F 1)",
+}
+
+
+def run_reorder(args):
+    """The reorder step alone on the R-MAT pattern: smat_reorder (this
+    library, host cores), or with --impl reference the reference's own
+    BlockingEngine built from its sources (oracle/_ref, single-threaded as
+    the reference runs it), where that build exists. Seconds per reorder,
+    and the permutation's hash so that the two arms can be compared."""
+    import smat
+    from smat import generators as G
+    A0 = G.rmat(16, 2_000_000, seed=3)
+    times, perm, extra = [], None, {}
+    for _ in range(max(args.steps, 1)):
+        t = time.perf_counter()
+        if args.impl == "reference":
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle as O
+            if not O.ref_available():
+                print(json.dumps({"impl": "reference", "workload": REORDER_WORKLOAD["workload"],
+                                  "unavailable": "the reference preprocess library is built only where the "
+                                                 "reference sources are (oracle/Makefile)"}), flush=True)
+                return
+            perm, _, st = O.ref_reorder(A0.row_ptr, A0.col_idx, A0.cols, 0.6, 16, 16)
+            extra = {"comparisons": int(st[0]), "merges": int(st[1]), "cores": 1}
+        else:
+            r = smat.reorder(A0, tau=0.6, col_block=16, row_block=16, algo=5, force_fixed=True)
+            perm = r.perm
+            extra = {"comparisons": int(r.comparisons), "merges": int(r.merges), "cores": os.cpu_count()}
+        times.append(time.perf_counter() - t)
+    line = {"metric": "reorder seconds", "value": float(np.median(times)), "unit": "s", "steps": len(times),
+            "higher_is_better": False, "data": "synthetic", "config": REORDER_WORKLOAD,
+            "perm_sha1": hashlib.sha1(np.ascontiguousarray(perm, np.int64).tobytes()).hexdigest()[:16]} | extra
+    if args.impl == "reference":
+        line["impl"] = "reference"
+    print(json.dumps(line), flush=True)
+
+
 def run_smat(args):
     import torch
 
@@ -440,6 +482,57 @@ def run_forms(args):
         del ws
 
 
+def run_libraries(args):
+    """Library comparison on the R-MAT workload: cuSPARSE CSR SpMM (through
+    torch.sparse.mm) on the same A and B as the headline line, one JSON line
+    per library configuration with its useful TFLOP/s and error vs FP64. A
+    reported comparison, not a target and not on the product path."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    A, _ = build_matrix()
+    N = WORKLOAD["N"]
+    Bh = np.random.default_rng(2).uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    import scipy.sparse as sps
+    ref = sps.csr_matrix((A.values.astype(np.float64), A.col_idx, A.row_ptr), shape=(A.rows, A.cols)) @ \
+        Bh.astype(np.float64)
+    nrm = np.linalg.norm(ref)
+    useful = 2.0 * A.nnz * N
+    crow = torch.from_numpy(A.row_ptr.astype(np.int32)).to(dev)
+    col = torch.from_numpy(A.col_idx.astype(np.int32)).to(dev)
+    for name, dt in (("cuSPARSE CSR SpMM, FP32 values and B (torch.sparse.mm)", torch.float32),
+                     ("cuSPARSE CSR SpMM, FP16 values and B (torch.sparse.mm)", torch.float16)):
+        try:
+            vals = torch.from_numpy(A.values.astype(np.float32)).to(dev, dt)
+            S = torch.sparse_csr_tensor(crow, col, vals, size=(A.rows, A.cols), device=dev)
+            B = torch.from_numpy(Bh).to(dev, dt)
+            out = torch.sparse.mm(S, B)
+            torch.cuda.synchronize(dev)
+        except Exception as e:  # a dtype the installed torch does not route to cuSPARSE
+            print(json.dumps({"metric": METRIC, "library": name, "unavailable": str(e).splitlines()[0][:200]}),
+                  flush=True)
+            continue
+        err = float(np.linalg.norm(out.double().cpu().numpy() - ref) / nrm)
+        for _ in range(max(args.warmup, 3)):
+            torch.sparse.mm(S, B)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            torch.sparse.mm(S, B)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        print(json.dumps({"metric": METRIC, "library": name, "value": useful / (ms * 1e-3) / 1e12,
+                          "unit": "TFLOP/s", "ms_per_step": ms, "rel_err_vs_fp64": err, "steps": args.steps,
+                          "warmup": args.warmup, "higher_is_better": True, "data": "synthetic",
+                          "config": {k: WORKLOAD[k] for k in ("workload", "generator", "N", "B", "C")} |
+                          {"nnz": A.nnz, "A": "CSR in the original row order (no reorder needed)",
+                           "step": "one torch.sparse.mm call"}}),
+              flush=True)
+        del S, B, out
+
+
 BATCH_WORKLOAD = {
     "workload": "batched512_uneven",
     "generator": "512 matrices, rows log-uniform in [1024, 32768]; 1/3 band (half-bandwidth 8-256), 1/3 R-MAT "
@@ -530,17 +623,24 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="smat", choices=["smat", "reference"])
-    ap.add_argument("--workload", default="rmat16", choices=["rmat16", "stencil64_forms", "batched512"],
+    ap.add_argument("--workload", default="rmat16",
+                    choices=["rmat16", "stencil64_forms", "batched512", "rmat16_libraries", "rmat16_reorder"],
                     help="rmat16: the headline SpMM line; stencil64_forms: one line per precision form; "
-                         "batched512: grouped vs sequential SpMMs")
+                         "batched512: grouped vs sequential SpMMs; rmat16_libraries: cuSPARSE on the "
+                         "headline inputs, for comparison; rmat16_reorder: the reorder step alone "
+                         "(with --impl reference: the reference's own reorder)")
     ap.add_argument("--batch-count", type=int, default=512)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "rmat16_reorder":
+        run_reorder(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "stencil64_forms":
         run_forms(args)
     elif args.workload == "batched512":
         run_batched(args)
+    elif args.workload == "rmat16_libraries":
+        run_libraries(args)
     else:
         run_smat(args)
 

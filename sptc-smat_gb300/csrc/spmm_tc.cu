@@ -56,8 +56,6 @@ namespace dev {
 
 enum : int { KIND_PLAIN = 0, KIND_SPLIT = 1, KIND_FP8 = 2 };
 
-// Stages between the L2 prefetch of a stage's A region and its copy.
-constexpr int kPrefetchAhead = 8;
 
 // Error sites recorded in the global error word.
 enum : int {
@@ -113,7 +111,7 @@ struct Cfg {
   // then the TMEM address, the abort flag, stage_ok[NS], the item ring and
   // the copy warps' current item
   static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 8 + 4 * (NS + kItemRing + 1);
-  static constexpr int THREADS = 512 + 32 * NCONV;
+  static constexpr int THREADS = 32 * (8 + NPROD + NCONV);  // MMA, epilogue, copy, converter warps
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
@@ -180,6 +178,12 @@ __device__ __forceinline__ bool take_item_warp(uint64_t* itemfull, uint64_t* ite
   return got != 0;
 }
 
+// The copy index that copy warp pw issues first in stage c: copy j of a
+// stage goes to warp (j + c) mod nprod, so the duties rotate.
+__device__ __forceinline__ int copy_of(int pw, uint32_t c, int nprod) {
+  return (int)(((uint32_t)pw + (uint32_t)nprod - c % (uint32_t)nprod) % (uint32_t)nprod);
+}
+
 __device__ __forceinline__ int shfl_i(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
   const int lo = __shfl_sync(0xffffffffu, (int)(uint32_t)(uint64_t)v, src);
@@ -187,8 +191,8 @@ __device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
   return (int64_t)(((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo);
 }
 
-// Warp roles (16 warps): 0..3 MMA issuers (0 also owns TMEM), 4..7
-// epilogue (TMEM lane quadrants 0..3), 8..15 copy warps.
+// Warp roles: 0..3 MMA issuers (0 also owns TMEM), 4..7 epilogue (TMEM lane
+// quadrants 0..3), then NPROD copy warps, then (FP8) the converter warps.
 template <int BH, int R, int NSUB, int KIND>
 __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
@@ -245,14 +249,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   int* err = args.err;
   const uint32_t smem0 = smem_u32(smem);
 
-  if (C::FP8 && warp >= 16) {
+  if (C::FP8 && warp >= 8 + C::NPROD) {
     // ------------------------------------------------------ FP8 converters
     // Each stage's e4m3 blocks and FP32 scales land in the staging area;
     // these four warps write them to the stage's A area as FP16 (value times
     // its block's scale, one rounding) in the 32-byte-swizzled layout the
     // MMA reads, make the writes visible to the tensor core's async proxy,
     // and release the stage to the MMA warps (conv barrier).
-    const int ct = threadIdx.x - 512;
+    const int ct = threadIdx.x - 32 * (8 + C::NPROD);
     uint32_t ci = 0;
     bool ok = true;
     for (uint32_t kk = 0; ok; ++kk) {
@@ -302,10 +306,11 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     // ---------------------------------------------------------------- copies
     // Stage number c (counted over the CTA's whole run) needs 1 + ntiles
     // bulk copies: copy 0 = the A blocks and the MMA list, copy j = B tile
-    // j - 1. Copy warp p issues the copies j with (j + c) % 8 == p (j and
-    // j + 8), so every warp issues one or two copies per stage and the A
-    // copy (from HBM, the slowest) rotates. A warp keeps only about one copy at a time in flight,
-    // so spreading them is what keeps the copy engine busy. The warp that
+    // j - 1. Copy warp p issues the copies j with (j + c) % NPROD == p (j and
+    // j + NPROD), so every warp issues one or two copies per stage and the A
+    // copy (from HBM, the slowest) rotates. A warp keeps only about one copy
+    // at a time in flight, so spreading them is what keeps the copy engine
+    // busy. The warp that
     // issues copy 0 posts the stage's total byte count (arrive.expect_tx) on
     // the stage's full barrier; the others only add their bytes as they land.
     // Stage records are read 32 at a time, one per lane, and each lane
@@ -348,57 +353,44 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
           const int cnt = min(32, wi.s1 - base);
           // lane l prepares stage ci + l
           const uint32_t my_ci = ci + (uint32_t)lane;
-          const int j0 = (int)(((uint32_t)pw - my_ci) & 7u);
-          int64_t off1 = 0, off2 = 0, pf_off = 0;
-          int bytes1 = 0, bytes2 = 0, dst1 = 0, dst2 = 0, total = 0, hword = 0, pf_bytes = 0;
+          const int j0 = copy_of(pw, my_ci, C::NPROD);
+          int64_t off1 = 0, off2 = 0;
+          int bytes1 = 0, bytes2 = 0, dst1 = 0, dst2 = 0, total = 0, hword = 0;
           if (lane < cnt) {
             const StageRec* rp = P.stages + stage0 + base + lane;
             const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
             const int4 r1 = reinterpret_cast<const int4*>(rp)[1];           // nblk, hdr_bytes, ntiles, -
             const int ntl = r1.z;
-            // this stage's A region, for the L2 prefetch
-            if (C::FP8) {
-              pf_off = r0.x * 256 + r1.w + r0.y;
-              pf_bytes = r1.x * 256 + fp8_scale_bytes(r1.x) + r1.y;
-            } else {
-              pf_off = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
-              pf_bytes = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
-            }
             if (j0 == 0) {
+              // the stage's A region (blocks, FP8 scales, header) in one copy
+              // (an L2 prefetch of it a few stages ahead measured slower:
+              // it competes with the copies for the copy engine)
+              if (C::FP8) {
+                off1 = r0.x * 256 + r1.w + r0.y;
+                bytes1 = r1.x * 256 + fp8_scale_bytes(r1.x) + r1.y;
+              } else {
+                off1 = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
+                bytes1 = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
+              }
               // header position inside the stage
               hword = C::FP8 ? (int)C::OFF_STG + r1.x * 256 + fp8_scale_bytes(r1.x) : r1.x * (int)(C::ABLK * C::NOPS);
-              off1 = pf_off;
-              bytes1 = pf_bytes;
               total = bytes1 + ntl * (int)C::TILEB;
             }
             // B copies, one per tile (several copies in flight land sooner
             // than one long copy of adjacent tiles): copy j >= 1 brings tile
-            // j - 1, this warp's are tiles j0 - 1 and j0 + 7
+            // j - 1, this warp's are tiles j0 - 1 and j0 + NPROD - 1
             if (j0 >= 1 && j0 <= ntl) {
               off1 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 - 1]) * (4096 * C::NOPS);
               bytes1 = (int)C::TILEB;
               dst1 = j0 - 1;
             }
-            if (j0 + 8 <= ntl) {
-              off2 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 + 7]) * (4096 * C::NOPS);
+            if (j0 + C::NPROD <= ntl) {
+              off2 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 + C::NPROD - 1]) * (4096 * C::NOPS);
               bytes2 = (int)C::TILEB;
-              dst2 = j0 + 7;
+              dst2 = j0 + C::NPROD - 1;
             }
-          }
-          // A comes from HBM: prefetch each stage's A region into L2 kPrefetchAhead
-          // stages before its copy (the batch's first stages right away, one per
-          // warp), so that the copy the MMA waits for is an L2 hit
-          if (pw < cnt && pw < kPrefetchAhead) {
-            const int64_t po = shfl_l(pf_off, pw);
-            const int pb = shfl_i(pf_bytes, pw);
-            if (lane == 0) bulk_prefetch_l2(P.aval + po, (uint32_t)pb);
           }
           for (int i = 0; i < cnt; ++i, ++ci) {
-            if (i + kPrefetchAhead < cnt) {
-              const int64_t po = shfl_l(pf_off, i + kPrefetchAhead);
-              const int pb = shfl_i(pf_bytes, i + kPrefetchAhead);
-              if (lane == 0 && (int)(((uint32_t)pw - ci) & 7u) == 0) bulk_prefetch_l2(P.aval + po, (uint32_t)pb);
-            }
             const int b1 = shfl_i(bytes1, i);
             const int b2 = shfl_i(bytes2, i);
             const int d1 = shfl_i(dst1, i);
@@ -407,7 +399,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
             const int64_t o2 = shfl_l(off2, i);
             const int tot = shfl_i(total, i);
             const int hw = shfl_i(hword, i);
-            const int j = (int)(((uint32_t)pw - ci) & 7u);
+            const int j = copy_of(pw, ci, C::NPROD);
             const uint32_t s = ci % C::NS;
             // The warp with copy 0 waits for the slot and passes its verdict
             // to the other copy warps through a named barrier (blocked warps

@@ -123,12 +123,6 @@ __device__ __forceinline__ void bulk_load_hint(uint32_t dst, const void* src, ui
       "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar), "l"(policy)
       : "memory");
 }
-// Bulk prefetch of global memory into L2 (no shared memory, no completion).
-// Address 16-byte aligned, size a multiple of 16.
-__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(src)), "r"(bytes)
-               : "memory");
-}
 __device__ __forceinline__ uint64_t make_l2_policy_evict_first() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
