@@ -184,6 +184,19 @@ __device__ __forceinline__ int copy_of(int pw, uint32_t c, int nprod) {
   return (int)(((uint32_t)pw + (uint32_t)nprod - c % (uint32_t)nprod) % (uint32_t)nprod);
 }
 
+// Bounded wait for a whole warp: lane 0 polls, the warp learns the outcome
+// by shuffle and leaves converged (lanes that each polled would leave the
+// loop on different iterations and could run the code after it diverged).
+__device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, int lane, volatile int* abort, int* err,
+                                          int where, bool sleepy) {
+  int got = 1;
+  if (lane == 0)
+    got = (sleepy ? wait_phase_sleepy(bar, parity, abort, err, where) : wait_phase(bar, parity, abort, err, where))
+              ? 1
+              : 0;
+  return __shfl_sync(0xffffffffu, got, 0) != 0;
+}
+
 __device__ __forceinline__ int shfl_i(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
   const int lo = __shfl_sync(0xffffffffu, (int)(uint32_t)(uint64_t)v, src);
@@ -272,7 +285,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
         for (int c = wi.s0; c < wi.s1; ++c, ++ci) {
           const uint32_t s = ci % C::NS;
-          if (!wait_phase(smem_u32(&full[s]), (ci / C::NS) & 1, abort_flag, err, ERR_CONV)) {
+          if (!warp_wait(smem_u32(&full[s]), (ci / C::NS) & 1, lane, abort_flag, err, ERR_CONV, false)) {
             ok = false;
             break;
           }
@@ -345,6 +358,12 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       }
       const WorkItem wi = args.items[idx];
       const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+      // fields used after shared-memory stores, held in registers (the stores
+      // could alias P for the compiler and force a reload each time)
+      const StageRec* const p_stages = P.stages;
+      const uint8_t* const p_aval = P.aval;
+      const uint8_t* const p_bpack = P.bpack;
+      const int64_t p_kbs = P.bp_kbs;
       const int n_tiles = P.n_tiles;
       const int stage0 = P.panels[wi.panel].stage_off;
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
@@ -357,7 +376,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
           int64_t off1 = 0, off2 = 0;
           int bytes1 = 0, bytes2 = 0, dst1 = 0, dst2 = 0, total = 0, hword = 0;
           if (lane < cnt) {
-            const StageRec* rp = P.stages + stage0 + base + lane;
+            const StageRec* rp = p_stages + stage0 + base + lane;
             const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
             const int4 r1 = reinterpret_cast<const int4*>(rp)[1];           // nblk, hdr_bytes, ntiles, -
             const int ntl = r1.z;
@@ -380,12 +399,12 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
             // than one long copy of adjacent tiles): copy j >= 1 brings tile
             // j - 1, this warp's are tiles j0 - 1 and j0 + NPROD - 1
             if (j0 >= 1 && j0 <= ntl) {
-              off1 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 - 1]) * (4096 * C::NOPS);
+              off1 = ((int64_t)bcol * p_kbs + rp->kb[j0 - 1]) * (4096 * C::NOPS);
               bytes1 = (int)C::TILEB;
               dst1 = j0 - 1;
             }
             if (j0 + C::NPROD <= ntl) {
-              off2 = ((int64_t)bcol * P.bp_kbs + rp->kb[j0 + C::NPROD - 1]) * (4096 * C::NOPS);
+              off2 = ((int64_t)bcol * p_kbs + rp->kb[j0 + C::NPROD - 1]) * (4096 * C::NOPS);
               bytes2 = (int)C::TILEB;
               dst2 = j0 + C::NPROD - 1;
             }
@@ -418,11 +437,11 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
                 } else if (j == 0) {
                   *reinterpret_cast<uint32_t*>(smem + s * C::STAGE + C::OFF_HW) = (uint32_t)hw;
                   mbar_arrive_expect_tx(fb, (uint32_t)tot);
-                  bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), P.aval + o1, (uint32_t)b1, fb, pol_a);
+                  bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), p_aval + o1, (uint32_t)b1, fb, pol_a);
                 } else {
-                  bulk_load_hint(st + C::OFF_B + d1 * C::TILEB, P.bpack + o1, (uint32_t)b1, fb, pol_b);
+                  bulk_load_hint(st + C::OFF_B + d1 * C::TILEB, p_bpack + o1, (uint32_t)b1, fb, pol_b);
                 }
-                if (b2 != 0) bulk_load_hint(st + C::OFF_B + d2 * C::TILEB, P.bpack + o2, (uint32_t)b2, fb, pol_b);
+                if (b2 != 0) bulk_load_hint(st + C::OFF_B + d2 * C::TILEB, p_bpack + o2, (uint32_t)b2, fb, pol_b);
                 if (b1 != 0 || b2 != 0) last_mine = ci;
               } else {
                 good = 0;
@@ -545,6 +564,11 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     }
     constexpr int SLAB = R * BH * C::BN;  // floats per slab
     constexpr int PW = (R % kMmaWarps == 0) ? R / kMmaWarps : 0;  // slots per issuing warp
+    constexpr int RPL = (R * BH + 31) / 32;                          // C-row entries per lane
+    // 16-row blocks with at least two slots per issuing warp: the drain reads
+    // two adjacent slots with one 32-column load (one load round trip per
+    // pair; a hub row's later parts are never in their first part's pair)
+    constexpr bool PAIR = BH == 16 && NSUB == 1 && PW >= 2 && R % 2 == 0;
     uint32_t k = 0;
     bool ok = true;
     for (uint32_t kk = 0; ok; ++kk) {
@@ -556,6 +580,13 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       if (idx < 0) break;
       const WorkItem wi = args.items[idx];
       const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+      // fields used between the stores to C, held in registers (the stores
+      // could alias P for the compiler and force reloads of every field)
+      const int p_N = P.N, p_nbr = P.nbr, p_f16 = P.c_f16;
+      const int64_t p_ldc = P.ldc;
+      void* const p_C = P.C;
+      float* const p_slabs = P.slabs;
+      int32_t* const p_counters = P.counters;
       const int n_tiles = P.n_tiles;
       const int panel = wi.panel;
       const bool split = wi.split >= 0;
@@ -563,36 +594,66 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       // a hub row cut over the issuing warps has its parts in slots s, s + PW,
       // s + 2 PW, ...; the parts after the first are added into it here
       const uint32_t ext_mask = P.panels[panel].ext_mask;
+      // the panel's C rows, plan row 32 q + lane in rmap[q] of that lane,
+      // loaded before the accumulators are ready: one global round trip
+      // per item instead of one per slot (the slot loops are unrolled, so
+      // rmap stays in registers)
+      int rmap[RPL];
+#pragma unroll
+      for (int q2 = 0; q2 < RPL; ++q2) {
+        const int pr = q2 * 32 + lane;
+        rmap[q2] = (pr < R * BH && (int64_t)panel * R * BH + pr < (int64_t)p_nbr * BH)
+                       ? P.row_map[(int64_t)panel * R * BH + pr]
+                       : -1;
+      }
       for (int nt = 0; nt < n_tiles; ++nt, ++k) {
         const uint32_t buf = k & 1;
-        if (!wait_phase_sleepy(smem_u32(&accfull[buf]), (k >> 1) & 1, abort_flag, err, ERR_EPI)) {
+        if (!warp_wait(smem_u32(&accfull[buf]), (k >> 1) & 1, lane, abort_flag, err, ERR_EPI, true)) {
           ok = false;
           break;
         }
         tc_fence_after();
         const uint32_t dbase = lane_base + buf * C::ACC_COLS;
         // slab of (part, column tile): (first slab of the panel + part) * n_tiles + nt
-        float* slab = split ? P.slabs + ((size_t)(wi.slab + wi.part) * n_tiles + nt) * SLAB : nullptr;
+        float* slab = split ? p_slabs + ((size_t)(wi.slab + wi.part) * n_tiles + nt) * SLAB : nullptr;
+        float pairv[32];
+#pragma unroll
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
-          if (rb >= P.nbr) break;
+          if (rb >= p_nbr) break;
+          if constexpr (PAIR) {
+            if ((s & 1) == 0) {
+              // slots s and s + 1 (an empty slot reads zeros: slots are
+              // zeroed after every drain and no MMA writes an empty one)
+              if ((slot_mask >> s) & 3u) {
+                const uint32_t ta = dbase + s * BH;
+                tmem_ld_x32(ta, pairv);
+                tmem_st_x32_zero(ta);
+              } else {
+#pragma unroll
+                for (int m = 0; m < 32; ++m) pairv[m] = 0.0f;
+              }
+            }
+          }
           if ((ext_mask >> s) & 1u) continue;
           const bool empty_slot = ((slot_mask >> s) & 1u) == 0;
-          const int myrow = (!split && lane < BH) ? P.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
             const int nl = j * 128 + (int)q * 32 + lane;  // column inside the tile
             const int n = nt * C::BN + nl;
 #pragma unroll
             for (int h = 0; h < BH; h += 16) {
-              float v[16];
-              if (!empty_slot) {
-                const uint32_t ta = dbase + j * C::SUB_COLS + s * BH + h;
-                tmem_ld_x16(ta, v);
-                tmem_st_x16_zero(ta);
-              } else {
+              float vs[16];
+              float* v = PAIR ? pairv + (s & 1) * 16 : vs;
+              if constexpr (!PAIR) {
+                if (!empty_slot) {
+                  const uint32_t ta = dbase + j * C::SUB_COLS + s * BH + h;
+                  tmem_ld_x16(ta, vs);
+                  tmem_st_x16_zero(ta);
+                } else {
 #pragma unroll
-                for (int m = 0; m < 16; ++m) v[m] = 0.0f;
+                  for (int m = 0; m < 16; ++m) vs[m] = 0.0f;
+                }
               }
               if constexpr (PW > 0) {
                 for (int t = s + PW; t < R && ((ext_mask >> t) & 1u); t += PW) {
@@ -611,13 +672,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               } else {
 #pragma unroll
                 for (int m = 0; m < 16; ++m) {
-                  const int row = __shfl_sync(0xffffffffu, myrow, h + m);
-                  if (row >= 0 && n < P.N) {
-                    const int64_t off = (int64_t)row * P.ldc + n;
-                    if (P.c_f16)
-                      __stcs(reinterpret_cast<__half*>(P.C) + off, __float2half_rn(v[m]));
+                  const int pr = s * BH + h + m;  // plan row inside the panel
+                  const int row = __shfl_sync(0xffffffffu, rmap[pr >> 5], pr & 31);
+                  if (row >= 0 && n < p_N) {
+                    const int64_t off = (int64_t)row * p_ldc + n;
+                    if (p_f16)
+                      __stcs(reinterpret_cast<__half*>(p_C) + off, __float2half_rn(v[m]));
                     else
-                      __stcs(reinterpret_cast<float*>(P.C) + off, v[m]);
+                      __stcs(reinterpret_cast<float*>(p_C) + off, v[m]);
                   }
                 }
               }
@@ -635,18 +697,18 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
         __syncwarp();
         int last = 0;
         if (lane == 0) {
-          int* ctr = P.counters + ((size_t)wi.split * n_tiles + nt) * 4 + q;
+          int* ctr = p_counters + ((size_t)wi.split * n_tiles + nt) * 4 + q;
           last = atomicAdd(ctr, 1) == wi.nparts - 1;
         }
         last = __shfl_sync(0xffffffffu, last, 0);
         if (!last) continue;
         __threadfence();
-        const float* slab0 = P.slabs + ((size_t)wi.slab * n_tiles + nt) * SLAB;
+        const float* slab0 = p_slabs + ((size_t)wi.slab * n_tiles + nt) * SLAB;
+#pragma unroll
         for (int s = 0; s < R; ++s) {
           const int rb = panel * R + s;
-          if (rb >= P.nbr) break;
+          if (rb >= p_nbr) break;
           if ((ext_mask >> s) & 1u) continue;  // added into its first part's slab rows
-          const int myrow = lane < BH ? P.row_map[(int64_t)rb * BH + lane] : -1;
 #pragma unroll
           for (int j = 0; j < NSUB; ++j) {
             const int nl = j * 128 + (int)q * 32 + lane;
@@ -668,13 +730,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               }
 #pragma unroll
               for (int m = 0; m < 16; ++m) {
-                const int row = __shfl_sync(0xffffffffu, myrow, h + m);
-                if (row >= 0 && n < P.N) {
-                  const int64_t off = (int64_t)row * P.ldc + n;
-                  if (P.c_f16)
-                    __stcs(reinterpret_cast<__half*>(P.C) + off, __float2half_rn(acc[m]));
+                const int pr = s * BH + h + m;
+                const int row = __shfl_sync(0xffffffffu, rmap[pr >> 5], pr & 31);
+                if (row >= 0 && n < p_N) {
+                  const int64_t off = (int64_t)row * p_ldc + n;
+                  if (p_f16)
+                    __stcs(reinterpret_cast<__half*>(p_C) + off, __float2half_rn(acc[m]));
                   else
-                    __stcs(reinterpret_cast<float*>(P.C) + off, acc[m]);
+                    __stcs(reinterpret_cast<float*>(p_C) + off, acc[m]);
                 }
               }
             }

@@ -95,7 +95,7 @@ struct WorkItem {
 
 // Everything the kernel needs about one SpMM problem.
 struct ProblemDesc {
-  const uint8_t* bpack;      // B in 4 KB tiles [k-block][128-column tile] (pack_b); the split
+  const uint8_t* bpack;      // B in 4 KB tiles [128-column tile][k-block] (pack_b); the split
                              // form stores [hi tile | lo tile] pairs, 8 KB per tile
   int64_t bp_kbs;            // k-blocks per 128-column tile in bpack ([column tile][k-block])
   const uint8_t* aval;       // A stream of the form (see StageRec)
