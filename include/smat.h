@@ -77,9 +77,9 @@ typedef struct smat_bcsr_opts {
   int32_t device;         /* CUDA device ordinal */
   int32_t panel_rows;     /* block rows per tensor-core panel: 4, 8 or 16 for bh 16, 4 or 8
                              for bh 32; 0 = the autotuner's cached choice for matrices
-                             like this one, else 128 rows (8, or 4 for bh 32) */
+                             like this one, else 256 rows (16, or 8 for bh 32) */
   float split_frac;       /* a panel costing more than split_frac x the average per-CTA
-                             work is split into parts over several CTAs (0 = default 1.0,
+                             work is split into parts over several CTAs (0 = default 0.5,
                              < 0 = never split) */
   const int64_t* col_perm;/* (host, optional) new column c = old column col_perm[c]: A is
                              blocked with its columns permuted (the reference's column

@@ -147,7 +147,7 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     int zero = 0;
     SMAT_TRY(upload(&h->d_err, &zero, 1));
   }
-  const double frac = split_frac == 0.0f ? 1.0 : (split_frac < 0.0f ? 1e30 : (double)split_frac);
+  const double frac = split_frac == 0.0f ? kDefaultSplitFrac : (split_frac < 0.0f ? 1e30 : (double)split_frac);
   for (int cls = 0; cls < kPlanClasses; cls++) {
     PlanDev& pd = h->pc[cls];
     if (!pd.built) continue;

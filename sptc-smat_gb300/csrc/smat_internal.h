@@ -167,9 +167,12 @@ inline int plan_class(int32_t form) {
   return form == SMAT_FORM_SPLIT_BF16 ? 1 : (form == SMAT_FORM_FP8 ? 2 : 0);
 }
 inline int plan_class_of_kind(int kind) { return kind == TC_KIND_SPLIT ? 1 : (kind == TC_KIND_FP8 ? 2 : 0); }
-// Block rows per panel when the caller leaves it to the library: 128 rows
-// (8 blocks of 16 rows, 4 of 32), two TMEM accumulator buffers of 128 columns.
-inline int default_panel_rows(int bh) { return bh == 16 ? 8 : 4; }
+// Block rows per panel when the caller leaves it to the library: 256 rows
+// (16 blocks of 16 rows, 8 of 32), two TMEM accumulator buffers of 256
+// columns; panels costing more than kDefaultSplitFrac of the average CTA
+// load are split into parts.
+inline int default_panel_rows(int bh) { return bh == 16 ? 16 : 8; }
+constexpr double kDefaultSplitFrac = 0.5;
 int pick_nsub(const smat_bcsr* h, int64_t N, int kind);
 
 // Workspace layout of one SpMM: [packed B (x2 for the split form)]

@@ -149,7 +149,7 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
         break;
       }
       const double t = ms / kReps;
-      if (R == default_panel_rows(bh) && f == 1.0f) ms_default = t;
+      if (R == default_panel_rows(bh) && f == (float)kDefaultSplitFrac) ms_default = t;
       if (t < best.ms) {
         best.ms = t;
         best.panel_rows = R;
