@@ -569,6 +569,11 @@ void build_work_items_multi(const std::vector<const Plan*>& plans, const std::ve
     }
   }
   double max_item = std::max(1.0, max_item_frac * total / std::max(1, workers));
+  // a part costs a full epilogue, a slab write and a share of the fixup
+  // whatever its size: never cut a panel into parts of fewer than
+  // kMinPartStages stages (small matrices then keep whole panels)
+  constexpr int32_t kMinPartStages = 4;
+  auto max_parts = [](int32_t nstages) { return std::max<int32_t>(1, nstages / kMinPartStages); };
   // bound the partial-sum slabs: at most kMaxSlabs parts of split panels per
   // problem (coarser parts where a problem would need more)
   constexpr int64_t kMaxSlabs = 96;
@@ -576,7 +581,8 @@ void build_work_items_multi(const std::vector<const Plan*>& plans, const std::ve
     for (int iter = 0; iter < 64; iter++) {
       int64_t parts_q = 0;
       for (int32_t p = 0; p < plans[q]->n_panels; p++) {
-        const int64_t parts = std::min<int64_t>((int64_t)std::ceil(pcost[q][p] / max_item), plans[q]->panels[p].nstages);
+        const int64_t parts = std::min<int64_t>((int64_t)std::ceil(pcost[q][p] / max_item),
+                                                max_parts(plans[q]->panels[p].nstages));
         if (parts > 1) parts_q += parts;
       }
       if (parts_q <= kMaxSlabs) break;
@@ -593,7 +599,7 @@ void build_work_items_multi(const std::vector<const Plan*>& plans, const std::ve
     for (int32_t p = 0; p < pl.n_panels; p++) {
       const PanelInfo& pi = pl.panels[p];
       int32_t parts = (int32_t)std::ceil(pcost[q][p] / max_item);
-      parts = std::max(1, std::min(parts, pi.nstages));
+      parts = std::max(1, std::min(parts, max_parts(pi.nstages)));
       if (parts == 1) {
         items.push_back(WorkItem{p, 0, pi.nstages, -1, 0, 1, 0, q});
         icost.push_back(pcost[q][p]);
