@@ -197,6 +197,7 @@ int run(const Case& cs, int bh, int R, int cls) {
       const PanelInfo& pi = pl.panels[w.panel];
       bad += check(w.s0 >= 0 && w.s0 < w.s1 && w.s1 <= pi.nstages, "item stage range");
       bad += check(w.split >= 0 || (w.s0 == 0 && w.s1 == pi.nstages), "an unsplit item is the whole panel");
+      bad += check(w.split < 0 || (w.nparts >= 2 && w.nparts <= pi.nstages / 4), "at most one part per four stages");
       for (int c = w.s0; c < w.s1; c++) stage_done[pi.stage_off + c]++;
       std::vector<double> acc((size_t)R * bh * N, 0.0);  // a part starts on zeroed accumulators
       bad += replay(hb, pl, R, cls, w.panel, w.s0, w.s1, B, N, acc, seen);
