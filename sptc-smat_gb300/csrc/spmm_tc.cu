@@ -567,8 +567,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     constexpr int RPL = (R * BH + 31) / 32;                          // C-row entries per lane
     // 16-row blocks with at least two slots per issuing warp: the drain reads
     // two adjacent slots with one 32-column load (one load round trip per
-    // pair; a hub row's later parts are never in their first part's pair)
-    constexpr bool PAIR = BH == 16 && NSUB == 1 && PW >= 2 && R % 2 == 0;
+    // pair; a hub row's later parts are never in their first part's pair).
+    // Not for FP8: its 640-thread CTAs have 96 registers a thread, and the
+    // pair's 32 values would spill.
+    constexpr bool PAIR = BH == 16 && NSUB == 1 && PW >= 2 && R % 2 == 0 && KIND != KIND_FP8;
     uint32_t k = 0;
     bool ok = true;
     for (uint32_t kk = 0; ok; ++kk) {
