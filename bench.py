@@ -182,7 +182,10 @@ def cpu_baseline(A, N, threads=1, budget_s=12.0, max_rows=None):
     target_nnz = budget_s / per_nnz * threads
     r1 = int(np.searchsorted(rp, target_nnz))
     r1 = max(1, min(rows, r1 if max_rows is None else min(r1, max_rows)))
-    bounds = np.linspace(0, r1, threads + 1).astype(np.int64)
+    # row ranges with equal nonzero counts (R-MAT rows differ by orders of
+    # magnitude, so equal row counts would leave one thread with the hubs)
+    bounds = np.searchsorted(rp, np.linspace(0, int(rp[r1]), threads + 1)).astype(np.int64)
+    bounds[0], bounds[-1] = 0, r1
     t = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         list(ex.map(lambda k: O.csr_multiply_f32_range(rows, int(bounds[k]), int(bounds[k + 1]), rp, ci, v, Bc, N,
