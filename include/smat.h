@@ -148,7 +148,8 @@ smat_status smat_csr_file_free(smat_csr_file* f);
  * identical to the reference's permutation; grouping_out (optional) receives
  * the final grouping vector (the reference's ".g" file content). A column
  * index is "the" column (col_idx); the pattern is used, values are ignored.
- * use_gpu is reserved (the scan runs on the host's cores either way). */
+ * The scan runs on the host's cores; use_gpu must be 0 (1 returns
+ * SMAT_ERR_UNSUPPORTED: there is no device scan). */
 smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
                          int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
                          int64_t* grouping_out, smat_reorder_stats* stats);
@@ -261,7 +262,9 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
  * exceeds that size (the packed B, K x N x 2 bytes or twice that for the
  * split form, plus the partial sums of panels split for load balance). The
  * first call on a device looks the array's address
- * up (make it before any stream capture). All calls on a device share the
+ * up (make it before any stream capture), and so does the first call after
+ * the device's context was destroyed and created again (cudaDeviceReset).
+ * All calls on a device share the
  * array: calls that overlap in time (other streams, other threads) race. */
 smat_status smat_spmm_static_scratch(const smat_bcsr* A, int32_t form, const void* B, int32_t b_dtype,
                                      int32_t b_layout, int64_t ldb, void* C, int32_t c_dtype, int64_t ldc,

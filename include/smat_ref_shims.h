@@ -7,10 +7,15 @@
  * FP16, C is M x N row-major FP16 (the reference's layouts).
  *
  * The first call for a matrix copies its BCSR arrays to the host and builds
- * a libsmat handle (cached on the device and array pointers, M, K and the
- * block count; the arrays must not change afterwards). Calls run on the
- * legacy default stream and return nothing; smat_ref_shims_last_status()
- * reports the last call's status.
+ * a libsmat handle, cached on the device, M, K, the block count and each
+ * array's address and allocation (buffer ID): arrays freed and allocated
+ * again are a new matrix, even at the same addresses, but contents rewritten
+ * in place are not noticed, so do not rewrite a cached matrix's arrays
+ * (smat_ref_shims_release() drops the cache). Calls run on the legacy
+ * default stream and return nothing; smat_ref_shims_last_status() reports
+ * the last call's status. The packed B goes to the library's static scratch
+ * when it fits (SMAT_SPMM_STATIC_SCRATCH_BYTES), else to a workspace kept
+ * with the cached handle and allocated by the first call that needs it.
  */
 #ifndef SMAT_REF_SHIMS_H_
 #define SMAT_REF_SHIMS_H_

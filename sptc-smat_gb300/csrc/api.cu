@@ -24,6 +24,17 @@ smat_status fail(smat_status st, const std::string& msg) {
   return st;
 }
 
+void* driver_fn(const char* name) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion(name, &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return fn;
+}
+
 static smat_status cuda_fail(cudaError_t e, const char* what) {
   return fail(SMAT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -264,8 +275,9 @@ const char* smat_version(void) { return "smat-gb300 0.1 (sm_103a, tcgen05)"; }
 smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
                          int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
                          int64_t* grouping_out, smat_reorder_stats* stats) {
-  (void)use_gpu;
   if (!A || !perm_out) return fail(SMAT_ERR_INVALID, "null argument");
+  if (use_gpu)
+    return fail(SMAT_ERR_UNSUPPORTED, "use_gpu: the reorder scan runs on the host's cores only (pass 0)");
   if (A->rows < 0 || !A->row_ptr || (A->nnz > 0 && !A->col_idx))
     return fail(SMAT_ERR_INVALID, "malformed CSR");
   if (col_block < 1 || row_block < 1) return fail(SMAT_ERR_INVALID, "block sizes must be >= 1");

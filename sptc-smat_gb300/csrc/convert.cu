@@ -8,7 +8,8 @@
 // n = 128*t .. 128*t+127 as 128 rows (one per n) of 16 16-bit k-values
 // (32 bytes each), in the 32-byte-swizzled shared-memory layout the MMA reads
 // (inside every 8-row group the two 16-byte halves of rows 4..7 are swapped).
-// Tiles are ordered [kb][t]; K is zero-padded to 16 and N to 128 (to 256
+// Tiles are ordered [t][kb] (column tile, then k-block: tile t*KB + kb);
+// K is zero-padded to 16 and N to 128 (to 256
 // when there is more than one tile, so that 256-column tiles stay in range).
 // The split form writes hi = bf16(b) and lo = bf16(b - hi) as one 8 KB
 // [hi tile | lo tile] pair per tile, so a tile is still one copy.

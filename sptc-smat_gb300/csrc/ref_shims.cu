@@ -6,12 +6,19 @@
 // The launchers receive device pointers to a BCSR matrix (values FP16
 // row-major per block, row pointers, column starts), B (K x N, column-major
 // FP16) and C (M x N, row-major FP16) and return nothing. The first call for
-// a given matrix (same device and array pointers, M, K and block count)
-// copies the BCSR to the host and builds a libsmat handle; later calls reuse
-// it, so the arrays must not change between calls (the reference's
-// SparseMatrix never changes them). Every call then runs
-// smat_spmm_static_scratch on the legacy default stream, like the reference
-// launchers, and so allocates nothing after the first call.
+// a given matrix copies the BCSR to the host and builds a libsmat handle;
+// later calls reuse it. The cache is keyed on the device, M, K, the block
+// count and, for every array, its address and the allocation's buffer ID
+// (CU_POINTER_ATTRIBUTE_BUFFER_ID, unique within the process): a matrix
+// freed and allocated again, even at the same addresses, is a new entry.
+// Contents changed in place are not detected, so the arrays must not be
+// rewritten while cached (the reference's SparseMatrix never rewrites
+// them); smat_ref_shims_release() drops every cached handle. Every call
+// then runs the SpMM on the legacy default stream, like the reference
+// launchers: through smat_spmm_static_scratch when the packed B fits its
+// fixed array (nothing allocated), else with a workspace kept beside the
+// cached handle, allocated on the first call that needs it (the stencil
+// shape, K = 262144 at N = 256, needs 128 MiB).
 //
 // The 2:4 variants take the reference's compressed values and metadata, but
 // compute from the uncompressed block values (which hold every block), so the
@@ -22,9 +29,11 @@
 // Errors cannot be returned through these signatures: the status of the last
 // shim call is kept (smat_ref_shims_last_status) and the message in
 // smat_last_error().
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <array>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -35,22 +44,74 @@
 
 namespace {
 
-using Key = std::tuple<int, const void*, const void*, const void*, size_t, size_t, size_t, int>;
+// (device, M, K, block count, block width, then address and buffer ID of
+// each array: values, row pointers, column starts, and the same three of the
+// dense part for the separate variant)
+using Key = std::tuple<int, size_t, size_t, size_t, int, std::array<uint64_t, 12>>;
+
+struct Entry {
+  smat_bcsr* h = nullptr;
+  void* ws = nullptr;  // workspace for packed B beyond the static scratch (device)
+  size_t ws_bytes = 0;
+};
 
 std::mutex g_mu;
-std::map<Key, smat_bcsr*> g_cache;
+std::map<Key, Entry> g_cache;
 smat_status g_last = SMAT_OK;
 
-// Handle for a device BCSR (16 x bw blocks), built on first sight.
-smat_status handle_for(const half* vals, const int* rowptr, const int* colidx, size_t M, size_t K, size_t nnzb,
-                       int bw, smat_bcsr** out) {
+// Unique ID of the allocation holding p (0 when the driver knows none).
+uint64_t buffer_id(const void* p) {
+  using PointerGetAttribute = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+  static const auto get_attr = reinterpret_cast<PointerGetAttribute>(smat::driver_fn("cuPointerGetAttribute"));
+  unsigned long long id = 0;
+  if (!p || !get_attr || get_attr(&id, CU_POINTER_ATTRIBUTE_BUFFER_ID, (CUdeviceptr)(uintptr_t)p) != CUDA_SUCCESS)
+    return 0;
+  return (uint64_t)id;
+}
+
+Key make_key(int dev, size_t M, size_t K, size_t nnzb, int bw, std::initializer_list<const void*> arrays) {
+  std::array<uint64_t, 12> a{};
+  size_t i = 0;
+  for (const void* p : arrays) {
+    a[i++] = (uint64_t)(uintptr_t)p;
+    a[i++] = buffer_id(p);
+  }
+  return Key{dev, M, K, nnzb, bw, a};
+}
+
+// The SpMM of a cached entry on the legacy default stream: the static
+// scratch when it is large enough, else the entry's own workspace.
+smat_status spmm_entry(Entry& e, const half* B, half* C, size_t N, size_t K) {
+  size_t need = 0;
+  smat_status st = smat_spmm_workspace_size(e.h, SMAT_FORM_F16, SMAT_F16, (int64_t)N, &need);
+  if (st != SMAT_OK) return st;
+  if (need <= (size_t)SMAT_SPMM_STATIC_SCRATCH_BYTES)
+    return smat_spmm_static_scratch(e.h, SMAT_FORM_F16, B, SMAT_F16, SMAT_COL_MAJOR, (int64_t)K, C, SMAT_F16,
+                                    (int64_t)N, (int64_t)N, nullptr);
+  if (need > e.ws_bytes) {
+    if (e.ws) cudaFree(e.ws);
+    e.ws = nullptr;
+    e.ws_bytes = 0;
+    if (cudaMalloc(&e.ws, need) != cudaSuccess) {
+      cudaGetLastError();
+      return smat::fail(SMAT_ERR_NOMEM, "workspace for the packed B: cudaMalloc failed");
+    }
+    e.ws_bytes = need;
+  }
+  return smat_spmm(e.h, SMAT_FORM_F16, B, SMAT_F16, SMAT_COL_MAJOR, (int64_t)K, C, SMAT_F16, (int64_t)N, (int64_t)N,
+                   e.ws, e.ws_bytes, nullptr);
+}
+
+// Cache entry for a device BCSR (16 x bw blocks), built on first sight.
+smat_status entry_for(const half* vals, const int* rowptr, const int* colidx, size_t M, size_t K, size_t nnzb,
+                      int bw, Entry** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaGetDevice failed");
-  const Key key{dev, vals, rowptr, colidx, M, K, nnzb, bw};
+  const Key key = make_key(dev, M, K, nnzb, bw, {vals, rowptr, colidx});
   std::lock_guard<std::mutex> lock(g_mu);
   auto it = g_cache.find(key);
   if (it != g_cache.end()) {
-    *out = it->second;
+    *out = &it->second;
     return SMAT_OK;
   }
   if (M % 16 || K % bw) return smat::fail(SMAT_ERR_INVALID, "M and K must be multiples of the block shape");
@@ -67,18 +128,20 @@ smat_status handle_for(const half* vals, const int* rowptr, const int* colidx, s
   smat_status st = smat_bcsr_create_from_bcsr((int64_t)M, (int64_t)K, 16, bw, (int64_t)nnzb, rp.data(), ci.data(),
                                               v.data(), &o, &h);
   if (st != SMAT_OK) return st;
-  g_cache[key] = h;
-  *out = h;
+  Entry& e = g_cache[key];
+  e.h = h;
+  *out = &e;
   return SMAT_OK;
 }
 
 void run(const half* vals, const int* rowptr, const int* colidx, const half* B, half* C, size_t M, size_t N, size_t K,
          size_t nnzb, int bw) {
-  smat_bcsr* h = nullptr;
-  smat_status st = handle_for(vals, rowptr, colidx, M, K, nnzb, bw, &h);
-  if (st == SMAT_OK)
-    st = smat_spmm_static_scratch(h, SMAT_FORM_F16, B, SMAT_F16, SMAT_COL_MAJOR, (int64_t)K, C, SMAT_F16,
-                                  (int64_t)N, (int64_t)N, nullptr);
+  Entry* e = nullptr;
+  smat_status st = entry_for(vals, rowptr, colidx, M, K, nnzb, bw, &e);
+  if (st == SMAT_OK) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    st = spmm_entry(*e, B, C, N, K);
+  }
   std::lock_guard<std::mutex> lock(g_mu);
   g_last = st;
 }
@@ -91,15 +154,16 @@ void run_separate(const half* vs, const int* rps, const int* cis, const half* vd
   smat_status st = SMAT_OK;
   int dev = 0;
   cudaGetDevice(&dev);
-  // the merged matrix is keyed on both parts' pointers
-  const Key key{dev, vs, vd, rps, M, K, (size_t)(const void*)rpd, bw};
-  smat_bcsr* h = nullptr;
+  // the merged matrix is keyed on both parts' arrays (block count 0: the
+  // parts' counts are in their row pointers)
+  const Key key = make_key(dev, M, K, 0, bw, {vs, rps, cis, vd, rpd, cid});
+  Entry* e = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);
     auto it = g_cache.find(key);
-    if (it != g_cache.end()) h = it->second;
+    if (it != g_cache.end()) e = &it->second;
   }
-  if (!h) {
+  if (!e) {
     const size_t nbr = M / 16, bsz = 16 * (size_t)bw;
     std::vector<int32_t> rp[2] = {std::vector<int32_t>(nbr + 1), std::vector<int32_t>(nbr + 1)};
     const int* rpp[2] = {rps, rpd};
@@ -145,18 +209,21 @@ void run_separate(const half* vs, const int* rps, const int* cis, const half* vd
       if (st == SMAT_OK) {
         smat_bcsr_opts o{};
         o.device = dev;
+        smat_bcsr* h = nullptr;
         st = smat_bcsr_create_from_bcsr((int64_t)M, (int64_t)K, 16, bw, (int64_t)mci.size(), mrp.data(), mci.data(),
                                         mv.data(), &o, &h);
         if (st == SMAT_OK) {
           std::lock_guard<std::mutex> lock(g_mu);
-          g_cache[key] = h;
+          e = &g_cache[key];
+          e->h = h;
         }
       }
     }
   }
-  if (st == SMAT_OK)
-    st = smat_spmm_static_scratch(h, SMAT_FORM_F16, B, SMAT_F16, SMAT_COL_MAJOR, (int64_t)K, C, SMAT_F16,
-                                  (int64_t)N, (int64_t)N, nullptr);
+  if (st == SMAT_OK) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    st = spmm_entry(*e, B, C, N, K);
+  }
   std::lock_guard<std::mutex> lock(g_mu);
   g_last = st;
 }
@@ -221,7 +288,10 @@ extern "C" smat_status smat_ref_shims_last_status(void) {
 
 extern "C" smat_status smat_ref_shims_release(void) {
   std::lock_guard<std::mutex> lock(g_mu);
-  for (auto& kv : g_cache) smat_bcsr_destroy(kv.second);
+  for (auto& kv : g_cache) {
+    if (kv.second.ws) cudaFree(kv.second.ws);
+    smat_bcsr_destroy(kv.second.h);
+  }
   g_cache.clear();
   return SMAT_OK;
 }

@@ -18,6 +18,12 @@ smat_status fail(smat_status st, const std::string& msg);
 // CUDA device ordinal a handle was built on (api.cu).
 int bcsr_device(const smat_bcsr* A);
 
+// A CUDA driver API function by name, looked up through the runtime
+// (cudaGetDriverEntryPointByVersion), or nullptr. libsmat does not link
+// libcuda, so that it loads (and its host-only entry points run) on machines
+// without a GPU driver.
+void* driver_fn(const char* name);
+
 // ------------------------------------------------------------------ reorder
 struct ReorderResult {
   std::vector<int64_t> grouping;

@@ -16,7 +16,11 @@
 // stands for the symbol, not a device address). The first call on each
 // device therefore looks the address up with cudaGetSymbolAddress, with
 // that device current, and keeps it for later calls on that device. Make
-// that first call on each device before any stream capture begins.
+// that first call on each device before any stream capture begins. The
+// address belongs to the device's primary context: every call compares that
+// context's ID with the one the address was looked up in, and looks it up
+// again when they differ (after cudaDeviceReset the module is loaded anew
+// and the array can move), so such a call also belongs outside a capture.
 //
 // Every call on a device shares the one array and leaves its contents
 // behind. The packed B is rewritten in full (padding included) by the pack
@@ -25,6 +29,7 @@
 // call's stream before each contraction. Calls that overlap in time — on
 // different streams, or from different threads — race on the array and
 // corrupt each other's results.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -41,22 +46,39 @@ static __device__ __align__(256) uint8_t g_spmm_scratch[SMAT_SPMM_STATIC_SCRATCH
 
 std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // ID of the context the address belongs to
 
-// Device address of g_spmm_scratch on `dev`, looked up once per device.
+// Device address of g_spmm_scratch on `dev`, looked up in the device's
+// current primary context (again whenever that context changed).
 smat_status scratch_on(int dev, void** out) {
   if (dev < 0 || dev >= kMaxDevices) return smat::fail(SMAT_ERR_UNSUPPORTED, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    int prev = -1;
-    if (cudaGetDevice(&prev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaGetDevice failed");
-    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaGetDevice failed");
+  // cudaSetDevice binds the device's primary context to this thread (also
+  // when dev is already current), so that the driver query below sees it
+  if (cudaSetDevice(dev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaSetDevice failed");
+  smat_status st = SMAT_OK;
+  using CtxGetCurrent = CUresult (*)(CUcontext*);
+  using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+  static const auto get_current = reinterpret_cast<CtxGetCurrent>(smat::driver_fn("cuCtxGetCurrent"));
+  static const auto get_id = reinterpret_cast<CtxGetId>(smat::driver_fn("cuCtxGetId"));
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) {
+    st = smat::fail(SMAT_ERR_CUDA, "no current CUDA context for the static scratch");
+  } else if (!g_scratch_addr[dev] || g_scratch_ctx[dev] != id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_scratch);
-    if (prev != dev) cudaSetDevice(prev);
-    if (e != cudaSuccess || !p)
-      return smat::fail(SMAT_ERR_CUDA, std::string("cudaGetSymbolAddress(g_spmm_scratch): ") + cudaGetErrorString(e));
-    g_scratch_addr[dev] = p;
+    if (e != cudaSuccess || !p) {
+      st = smat::fail(SMAT_ERR_CUDA, std::string("cudaGetSymbolAddress(g_spmm_scratch): ") + cudaGetErrorString(e));
+    } else {
+      g_scratch_addr[dev] = p;
+      g_scratch_ctx[dev] = id;
+    }
   }
+  if (prev != dev) cudaSetDevice(prev);
+  if (st != SMAT_OK) return st;
   *out = g_scratch_addr[dev];
   return SMAT_OK;
 }

@@ -66,9 +66,12 @@ def rand_pattern(rng, rows, cols, deg, shuffle=False):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("SMAT_REFERENCE"),
+                    help="reference source tree (default: $SMAT_REFERENCE, else the oracle recipe's default)")
     args = ap.parse_args()
     import oracle as O
+    if args.reference:
+        os.environ["SMAT_REFERENCE"] = args.reference
     O.build(ref=True)
     if not O.ref_available():
         raise SystemExit("reference build not available")

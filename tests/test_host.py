@@ -54,6 +54,13 @@ def test_reorder_fixed_blocking(smat_mod):
     assert r.perm.tolist() == list(range(10))
 
 
+def test_reorder_rejects_device_scan_request(smat_mod):
+    A = smat_mod.Csr(10, 10, np.arange(11), np.arange(10))
+    with pytest.raises(smat_mod.SmatError) as e:
+        smat_mod.reorder(A, 0.5, 4, 4, use_gpu=True)
+    assert "use_gpu" in str(e.value)
+
+
 def test_reorder_empty_rows_and_matrix(smat_mod):
     A = smat_mod.Csr(5, 8, np.zeros(6, np.int64), np.zeros(0, np.int32))
     r = smat_mod.reorder(A, 0.5, 4, 2)

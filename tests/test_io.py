@@ -100,7 +100,6 @@ def test_write_el_round_trip(smat_mod, tmp_path):
     assert np.array_equal(B.col_idx, P.col_idx)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference sources absent")
 def test_readers_match_reference_live(smat_mod, oracle_lib, tmp_path):
     if not oracle_lib.ref_available():
         pytest.skip("reference build unavailable")

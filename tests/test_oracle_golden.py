@@ -78,7 +78,6 @@ def test_fp64_oracle_matches_scipy(oracle_lib):
     assert np.allclose(C, m @ B, rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference sources absent")
 def test_oracle_matches_reference_live(oracle_lib):
     if not oracle_lib.ref_available():
         pytest.skip("reference build unavailable")

@@ -2,8 +2,9 @@
 device array, nothing allocated) against smat_spmm (caller workspace), both
 called through the C ABI, on two calls in a row with different B, N and
 form, so that the second call runs over the first call's leftovers. Also
-checked against the FP64 oracle (FP16 form: 1e-3; split form: 1e-4) and the
-rejection of a B too large for the array.
+checked against the FP64 oracle (FP16 form: 1e-3; split form: 1e-4), that
+repeated calls leave the device's free memory unchanged (no allocation on the
+path), and the rejection of a B too large for the array.
 
 The file name sorts last so the test also runs after the whole GPU suite.
 """
@@ -70,6 +71,33 @@ def test_static_scratch_matches_workspace_entry_point(dev, smat_mod, oracle_lib)
     np.testing.assert_allclose(Cs, Cr, rtol=1e-6, atol=1e-6)
     ref2 = oracle_lib.spmm_f64(*A64, B2.astype(np.float64))
     assert rel_err(Cs, ref2) <= 1e-4
+
+
+def test_static_scratch_allocates_nothing(dev, smat_mod):
+    from smat import generators as G
+    A = G.rmat(12, 60_000, seed=5)
+    M = smat_mod.Bcsr(A, forms=(smat_mod.FORM_F16,))
+    L = smat_mod._lib.lib()
+    N = 256
+    B = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, (A.cols, N)).astype(np.float16)).to(dev)
+    Cm = torch.empty((A.rows, N), dtype=torch.float32, device=dev)
+    s = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        st = L.smat_spmm_static_scratch(M.handle, smat_mod.FORM_F16, C.c_void_p(B.data_ptr()), smat_mod.F16,
+                                        smat_mod.ROW_MAJOR, N, C.c_void_p(Cm.data_ptr()), smat_mod.F32, N, N,
+                                        C.c_void_p(s))
+        assert st == 0, L.smat_last_error().decode()
+
+    call()                                                   # the first call looks the array's address up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(50):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    M.check_device_error()
+    assert free1 == free0
 
 
 def test_static_scratch_rejects_oversized_b(dev, smat_mod):
