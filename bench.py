@@ -37,7 +37,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sptc-smat_gb300"))
 
 METRIC = "SpMM useful TFLOP/s, chosen form vs plain FP16 BCSR on one GB300 at stated rel err"
-CACHE = os.environ.get("SMAT_CACHE", os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "bench_cache"))
 
 WORKLOAD = {
     "workload": "rmat16_2M_reordered_tau0.6_bcsr16x16_24frac0.3_N128",
@@ -61,28 +60,19 @@ def log(*a):
 # ---------------------------------------------------------------------------------------------- workload
 
 def build_matrix():
-    """(A in original row order, perm, nnz) for the R-MAT workload; the reorder is cached on disk."""
-    import smat
-    from smat import generators as G
+    """(A in original row order, perm) for the R-MAT workload (smat.workloads.rmat16; the reorder is cached on
+    disk)."""
+    from smat import workloads
 
     t0 = time.time()
-    A0 = G.rmat(16, 2_000_000, seed=3)
-    key = hashlib.sha1(A0.row_ptr.tobytes() + A0.col_idx.tobytes()).hexdigest()[:16]
-    os.makedirs(CACHE, exist_ok=True)
-    pfile = os.path.join(CACHE, f"perm_{key}_t0.6_b16_B16.npy")
-    if os.path.exists(pfile):
-        perm = np.load(pfile)
-    else:
-        r = smat.reorder(A0, tau=0.6, col_block=16, row_block=16, algo=5, force_fixed=True)
-        perm = r.perm
-        np.save(pfile, perm)
-    Ar = A0.permuted(perm)                       # reordered row order
-    Ar = G.force_24(Ar, 0.3, 16, 16, seed=6)     # exact 2:4 in 30 % of the blocks
-    inv = np.empty_like(perm)
-    inv[perm] = np.arange(perm.size)
-    A = Ar.permuted(inv)                         # back to the original row order
+    A, perm = workloads.rmat16()
     log(f"[bench] matrix ready in {time.time() - t0:.1f}s: nnz={A.nnz}")
     return A, perm
+
+
+def workload_config(A, world):
+    """The `config` of the R-MAT line, identical in both arms."""
+    return dict(WORKLOAD, nnz=int(A.nnz), parallelism=f"replicas x{world}" if world > 1 else "single GPU")
 
 
 # ---------------------------------------------------------------------------------------------- clocks
@@ -229,7 +219,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": WORKLOAD,
+            "data": "synthetic", "config": workload_config(A, world),
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                              "sample": sample + "; reference CSR::multiply loop (csr.cpp:47-63), row ranges on "
                                                 f"{threads} threads"},
@@ -406,8 +396,9 @@ def run_smat(args):
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f16", "data": "synthetic",
-        "config": dict(WORKLOAD, nnz=nnz, nnzb=nnzb, fill=info["fill"], n_union_cols=info["n_union_cols"],
-                       panel_rows=info["panel_rows"], parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "config": workload_config(A, world),
+        "matrix": {"nnzb": nnzb, "fill": info["fill"], "n_union_cols": info["n_union_cols"],
+                   "n_blocks_24": info["n_blocks_24"], "panel_rows": info["panel_rows"]},
         "rel_err_vs_fp64": rel_err,
         "stored_tflops": world * stored / (ms * 1e-3) / 1e12,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -448,9 +439,9 @@ def run_forms(args):
     import torch
 
     import smat
-    from smat import generators as G
+    from smat import workloads
     dev = torch.device("cuda", 0)
-    A = G.stencil27(64, seed=4)
+    A = workloads.stencil64()
     N = FORMS_WORKLOAD["N"]
     forms = {"f16": smat.FORM_F16, "bf16": smat.FORM_BF16, "fp8": smat.FORM_FP8, "split_bf16": smat.FORM_SPLIT_BF16}
     t0 = time.time()
@@ -562,25 +553,14 @@ def run_batched(args):
     import torch
 
     import smat
-    from smat import generators as G
+    from smat import workloads
     dev = torch.device("cuda", 0)
-    rng = np.random.default_rng(11)
     count = args.batch_count
     t0 = time.time()
     probs = []
     useful = 0.0
-    for i in range(count):
-        rows = int(np.exp(rng.uniform(np.log(1024), np.log(32768))))
-        fam = i % 3
-        if fam == 0:
-            A = G.band(rows, int(np.exp(rng.uniform(np.log(8), np.log(256)))), seed=i)
-        elif fam == 1:
-            scale = int(np.ceil(np.log2(rows)))
-            A = G.rmat(scale, int(rng.uniform(8, 64) * (1 << scale)), seed=i)
-        else:
-            A = G.random_block(rows, float(rng.uniform(0.01, 0.05)), 0.4, 0.9, seed=i)
-        N = int(rng.choice([32, 64, 128]))
-        form = smat.FORM_F16 if i % 2 == 0 else smat.FORM_BF16
+    for A, N, fk in workloads.batched512(count):
+        form = smat.FORM_F16 if fk == 0 else smat.FORM_BF16
         tdt = torch.float16 if form == smat.FORM_F16 else torch.bfloat16
         M = smat.Bcsr(A, forms=(form,))
         B = torch.randn((A.cols, N), device=dev).to(tdt)

@@ -363,9 +363,25 @@ smat_status smat_spmm_host(const smat_bcsr* A, int32_t form, const void* B_host,
                            int64_t ldc, int64_t N, void* stream);
 
 /* Reads and clears the handle's device-side error word, which the kernels
- * set when a bounded wait expires (then SMAT_ERR_TIMEOUT is returned). Call
- * after synchronising the stream the SpMM ran on. */
+ * set when a bounded wait expires (then SMAT_ERR_TIMEOUT is returned, and
+ * smat_last_error() names the wait's site). Call after synchronising the
+ * stream the SpMM ran on. */
 smat_status smat_bcsr_check_device_error(const smat_bcsr* A);
+
+/* Limit, in nanoseconds, of every device-side wait in this handle's SpMM
+ * launches (0: the default, 4 s). A wait that runs out aborts the launch:
+ * the kernel drains its own copies and MMAs, frees its tensor memory and
+ * returns, and smat_bcsr_check_device_error reports SMAT_ERR_TIMEOUT; the
+ * handle stays usable. No counterpart in the reference, whose waits are
+ * unbounded. */
+smat_status smat_bcsr_set_wait_limit(smat_bcsr* A, uint64_t ns);
+
+/* Testing hook for the path above: the next SpMM launch on A makes the
+ * first MMA-issuing thread of CTA 0 wait, before its stage-th stage
+ * (1-based), on a barrier that nothing arrives at, so that its bounded
+ * wait runs out (site 205) without any fault. 0 cancels. No counterpart in
+ * the reference. */
+smat_status smat_bcsr_debug_stall(smat_bcsr* A, int32_t stage);
 
 const char* smat_last_error(void);
 const char* smat_version(void);

@@ -51,6 +51,12 @@ void mmaOBTSKernel_large_separate(half* bcsrValuesA_sparse, int* bcsrRowPtrA_spa
  * of the blocks blockInfo marks 1, into its own metadata / value layout. */
 void preprocessing_mmaSTKernel(half* bcsrValuesA, char* metadata, half* sparseMatrixA, size_t M, size_t N, size_t K,
                                size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping);
+/* mmaST_large.cu:22-152 launcher :324-335 (main.cu:64-68): the same for 16 x 32
+ * blocks (two metadata bytes and eight values per lane); the launcher that
+ * main.cu:306-311 hands to evaluateSparse24_2 and evaluateSplit. */
+void preprocessing_mmaSTKernel_large(half* bcsrValuesA, char* metadata, half* sparseMatrixA, size_t M, size_t N,
+                                     size_t K, size_t nonzeroBlocks, int* blockInfo,
+                                     int* relativeBlockIndexMapping);
 #endif
 
 #ifdef __cplusplus

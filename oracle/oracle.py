@@ -73,6 +73,19 @@ def lib():
     return _lib
 
 
+def reference_dir():
+    """The reference source tree: $SMAT_REFERENCE, else the one the last
+    oracle build compiled from (oracle/_ref/source_dir.txt); None when
+    neither names an existing directory."""
+    d = os.environ.get("SMAT_REFERENCE")
+    if not d:
+        p = os.path.join(REFDIR, "source_dir.txt")
+        if os.path.exists(p):
+            with open(p) as f:
+                d = f.read().strip()
+    return d if d and os.path.isdir(d) else None
+
+
 def ref_available() -> bool:
     return os.path.exists(os.path.join(REFDIR, "libsmat_ref_preprocess.so"))
 

@@ -25,8 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", f"-I{INCLUDE}", f"-I{CSRC}"]
 HOSTFLAGS = ["-fPIC", "-fopenmp", "-ffp-contract=off"]
 
-CU_SOURCES = ["api.cu", "spmm_tc.cu", "convert.cu", "spmm_static.cu", "ref_shims.cu", "spmm_24ref.cu", "group.cu", "tune.cu", "features.cu", "mlp.cu"]
-CPP_SOURCES = ["reorder.cpp", "bcsr.cpp", "io.cpp"]
+CU_SOURCES = ["api.cu", "spmm_tc.cu", "spmm24.cu", "convert.cu", "spmm_static.cu", "ref_shims.cu", "spmm_24ref.cu", "group.cu", "tune.cu", "features.cu", "mlp.cu"]
+CPP_SOURCES = ["reorder.cpp", "bcsr.cpp", "sp24.cpp", "io.cpp"]
 
 
 def _cmd_cu(src, obj):
@@ -68,7 +68,7 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
-        run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lcuda"])
+        run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp"])
     return LIB
 
 

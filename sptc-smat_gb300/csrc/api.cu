@@ -78,7 +78,8 @@ static void free_handle(smat_bcsr* h) {
   cudaGetDevice(&prev);
   cudaSetDevice(h->device);
   void* ptrs[] = {h->d_kperm, h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
-                  h->d_bstage, h->d_cstage, h->d_ws};
+                  h->d_bstage, h->d_cstage, h->d_ws, h->d_sp24_stages, h->d_sp24_groups,
+                  h->d_sp24_unit_window, h->d_sp24_stream[0], h->d_sp24_stream[1], h->d_bcsr_row_map};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (PlanDev& pd : h->pc) {
@@ -130,10 +131,15 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   h->R = R;
   // class 0 serves the FP16 and BF16 forms (and the handle's info), class 1
   // the split form, class 2 the FP8 form
+  // the structured-sparse path takes the exact-2:4 blocks of the FP16 and
+  // BF16 forms (16 x 16 blocks); their plan (class 0) leaves them out
+  h->sp24_on = h->use24 && bh == 16 && bw == 16 &&
+               (forms & ((1u << SMAT_FORM_F16) | (1u << SMAT_FORM_BF16))) &&
+               std::any_of(h->host.is24.begin(), h->host.is24.end(), [](uint8_t v) { return v != 0; });
   for (int cls = 0; cls < kPlanClasses; cls++) {
     if (cls == 1 && !(forms & (1u << SMAT_FORM_SPLIT_BF16))) continue;
     if (cls == 2 && !(forms & (1u << SMAT_FORM_FP8))) continue;
-    st = build_plan(h->host, R, cls, h->pc[cls].plan);
+    st = build_plan(h->host, R, cls, h->pc[cls].plan, (cls == 0 && h->sp24_on) ? &h->host.is24 : nullptr);
     if (st != SMAT_OK) {
       delete h;
       return st;
@@ -141,7 +147,7 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     h->pc[cls].built = true;
   }
   for (uint8_t v : h->host.is24) h->n_24 += v;
-  if (!h->use24) h->n_24 = 0;
+  if (!h->sp24_on) h->n_24 = 0;
 
 #define SMAT_TRY(x)              \
   do {                           \
@@ -154,6 +160,21 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
 
   const HostBcsr& b = h->host;
   if (!b.kperm.empty()) SMAT_TRY(upload(&h->d_kperm, b.kperm.data(), b.kperm.size()));
+  if (h->sp24_on) {
+    Sp24Host sp;
+    for (int fmt = 0; fmt < 2; fmt++) {
+      if (!(forms & (1u << (fmt == 0 ? SMAT_FORM_F16 : SMAT_FORM_BF16)))) continue;
+      SMAT_TRY(build_sp24(b, b.is24, fmt, sp));
+      SMAT_TRY(upload(&h->d_sp24_stream[fmt], sp.stream.data(), sp.stream.size()));
+    }
+    // (some block is exactly 2:4, so every list below has an entry)
+    SMAT_TRY(upload(&h->d_sp24_stages, sp.stages.data(), sp.stages.size()));
+    SMAT_TRY(upload(&h->d_sp24_groups, sp.groups.data(), sp.groups.size()));
+    SMAT_TRY(upload(&h->d_sp24_unit_window, sp.unit_window.data(), sp.unit_window.size()));
+    SMAT_TRY(upload(&h->d_bcsr_row_map, b.row_map.data(), b.row_map.size()));
+    h->sp24_ngroups = (int32_t)sp.groups.size();
+    h->sp24_units = sp.n_units;
+  }
   {
     int zero = 0;
     SMAT_TRY(upload(&h->d_err, &zero, 1));
@@ -464,11 +485,20 @@ smat_status smat_csr_to_bcsr_host(const smat_csr* A, int32_t block_rows, int32_t
 
 }  // extern "C"
 
+// The 2:4 path runs for this form (the exact-2:4 blocks are not in its plan).
+static bool uses_sp24(const smat_bcsr* A, int32_t form) {
+  return A->sp24_on && (form == SMAT_FORM_F16 || form == SMAT_FORM_BF16);
+}
+
 WsLayout smat::ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
   WsLayout w;
   const bool split = form == SMAT_FORM_SPLIT_BF16;
   const size_t one = (packed_b_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
   w.counters = split ? 2 * one : one;
+  if (uses_sp24(A, form)) {
+    w.b64 = w.counters;
+    w.counters += (packed_b64_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
+  }
   const int nsub = pick_nsub(A, N, kind_of(form));
   const Sched& sc = A->pc[plan_class(form)].sched[nsub];
   const int64_t bn = 128 * nsub, n_tiles = (std::max<int64_t>(N, 1) + bn - 1) / bn;
@@ -591,6 +621,11 @@ smat_status smat_spmm_pack_b(const smat_bcsr* A, int32_t form, const void* B, in
   cudaError_t e = pack_b(B, in_dt, b_layout == SMAT_COL_MAJOR ? 1 : 0, ldb, mode, out, K, N, A->d_kperm,
                          static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "pack_b");
+  if (uses_sp24(A, form)) {
+    const WsLayout wl = ws_layout(A, form, N);
+    e = pack_b_sw64(out, K, N, out + wl.b64, static_cast<cudaStream_t>(stream_));
+    if (e != cudaSuccess) return cuda_fail(e, "pack_b_sw64");
+  }
   return SMAT_OK;
 }
 
@@ -618,6 +653,8 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   args.n_items = sc.n_items;
   args.items = sc.d_items;
   args.err = A->d_err;
+  args.wait_ns = A->wait_ns;
+  args.stall_stage = const_cast<smat_bcsr*>(A)->stall.exchange(0);
   uint8_t* ctr = static_cast<uint8_t*>(const_cast<void*>(packed_b)) + wl.counters;
   args.next_item = reinterpret_cast<int32_t*>(ctr);
   {
@@ -628,6 +665,33 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   }
   cudaError_t e = tc_launch(bh, R, nsub, kind, args, sc.grid, static_cast<cudaStream_t>(stream_));
   if (e != cudaSuccess) return cuda_fail(e, "spmm kernel launch");
+  if (uses_sp24(A, form)) {
+    // the exact-2:4 blocks, added into the C the dense kernel wrote
+    Sp24Args a24;
+    std::memset(&a24, 0, sizeof(a24));
+    const int fmt = form == SMAT_FORM_BF16 ? 1 : 0;
+    a24.stream = A->d_sp24_stream[fmt];
+    a24.stages = A->d_sp24_stages;
+    a24.groups = A->d_sp24_groups;
+    a24.unit_window = A->d_sp24_unit_window;
+    a24.row_map = A->d_bcsr_row_map;
+    a24.bpack64 = static_cast<const uint8_t*>(packed_b) + wl.b64;
+    a24.kw = ((hb.cols + 15) / 16 + 1) / 2;
+    a24.C = C;
+    a24.ldc = ldc;
+    a24.N = (int32_t)N;
+    a24.n_tiles = (int32_t)((N + 127) / 128);
+    a24.n_groups = A->sp24_ngroups;
+    a24.c_f16 = c_dtype == SMAT_F16 ? 1 : 0;
+    // kind::f16 instruction descriptor without N: sparse (bit 2), FP32
+    // accumulator, A and B FP16 (0) or BF16 (1), K-major, M = 128
+    a24.idesc = (1u << 2) | (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(128 >> 4) << 24);
+    a24.err = A->d_err;
+    a24.wait_ns = A->wait_ns;
+    const int grid = std::max(1, std::min<int>(A->num_sms, A->sp24_ngroups));
+    e = sp24_launch(a24, grid, static_cast<cudaStream_t>(stream_));
+    if (e != cudaSuccess) return cuda_fail(e, "2:4 spmm kernel launch");
+  }
   return SMAT_OK;
 }
 
@@ -691,6 +755,19 @@ smat_status smat_spmm_host(const smat_bcsr* A_, int32_t form, const void* B_host
   if (s != SMAT_OK) return s;
   SMAT_CUDA(cudaMemcpyAsync(C_host, A->d_cstage, cbytes, cudaMemcpyDeviceToHost, stream));
   SMAT_CUDA(cudaStreamSynchronize(stream));
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_set_wait_limit(smat_bcsr* A, uint64_t ns) {
+  if (!A) return fail(SMAT_ERR_INVALID, "null argument");
+  A->wait_ns = ns;
+  return SMAT_OK;
+}
+
+smat_status smat_bcsr_debug_stall(smat_bcsr* A, int32_t stage) {
+  if (!A) return fail(SMAT_ERR_INVALID, "null argument");
+  if (stage < 0) return fail(SMAT_ERR_INVALID, "stage must be >= 0");
+  A->stall.store(stage);
   return SMAT_OK;
 }
 

@@ -305,7 +305,7 @@ smat_status quantize_fp8(const HostBcsr& b, std::vector<uint8_t>& q, std::vector
   return SMAT_OK;
 }
 
-smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
+smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan, const std::vector<uint8_t>* skip) {
   if (R < 1 || R > 32) return fail(SMAT_ERR_INVALID, "panel rows must be in [1, 32]");
   const int64_t nbr = b.nbr();
   plan.R = R;
@@ -429,7 +429,8 @@ smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
       uint32_t mask = 0;
       for (int32_t sl = 0; sl < R; sl++) {
         if (S[sl].k1 > S[sl].k0) mask |= 1u << sl;
-        for (int32_t k = S[sl].k0; k < S[sl].k1; k += S[sl].step) ent.push_back({(int64_t)b.colidx[k] * 32 + sl, k});
+        for (int32_t k = S[sl].k0; k < S[sl].k1; k += S[sl].step)
+          if (!skip || !(*skip)[k]) ent.push_back({(int64_t)b.colidx[k] * 32 + sl, k});
       }
       L.info.ext_mask = ext_masks[p];
       std::sort(ent.begin(), ent.end());
@@ -501,8 +502,9 @@ smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan) {
           std::memcpy(h + kStageHdrFixed + 4 * i, &mma[i].second, 4);
         }
         std::memcpy(h, wl, sizeof(wl));
-        const uint16_t nb16 = (uint16_t)s.nblk;
+        const uint16_t nb16 = (uint16_t)s.nblk, nt16 = (uint16_t)s.ntiles;
         std::memcpy(h + 8, &nb16, 2);
+        std::memcpy(h + 10, &nt16, 2);
         L.stages.push_back(s);
       }
       L.info.nstages = (int32_t)L.stages.size();

@@ -176,7 +176,48 @@ static cudaError_t run_pack(const void* in, int layout, int64_t ldi, uint8_t* ou
   return cudaGetLastError();
 }
 
+// The 2:4 path's B operand from the packed tiles: tile (t, w) holds k-blocks
+// 2w and 2w+1 of column tile t side by side, 128 rows (n) of 64 bytes (32
+// k-values) in the 64-byte swizzle (inside every 8-row group, 16-byte chunk
+// c of row n sits at chunk c ^ ((n >> 1) & 3)). One thread per row.
+__global__ void pack_b_sw64_kernel(const uint8_t* __restrict__ p32, uint8_t* __restrict__ out, int64_t kbs,
+                                   int64_t kw) {
+  const int64_t w = blockIdx.x;
+  const int64_t t = blockIdx.y;
+  const int n = threadIdx.x;
+  uint4 c[4];
+#pragma unroll
+  for (int hb = 0; hb < 2; ++hb) {
+    const int64_t kb = 2 * w + hb;
+    if (kb < kbs) {
+      const uint4* src = reinterpret_cast<const uint4*>(p32 + (t * kbs + kb) * 4096 + n * 32);
+      const int sw = (n >> 2) & 1;
+      c[2 * hb] = src[sw];
+      c[2 * hb + 1] = src[sw ^ 1];
+    } else {
+      c[2 * hb] = c[2 * hb + 1] = make_uint4(0, 0, 0, 0);
+    }
+  }
+  uint4* dst = reinterpret_cast<uint4*>(out + (t * kw + w) * 8192 + n * 64);
+  const int sw = (n >> 1) & 3;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dst[q ^ sw] = c[q];
+}
+
 }  // namespace dev
+
+size_t packed_b64_bytes(int64_t K, int64_t N) {
+  const int64_t kw = ((K + 15) / 16 + 1) / 2;
+  return (size_t)kw * (size_t)packed_b_tiles(N) * 8192;
+}
+
+cudaError_t pack_b_sw64(const uint8_t* packed32, int64_t K, int64_t N, uint8_t* out, cudaStream_t s) {
+  const int64_t kbs = (K + 15) / 16, kw = (kbs + 1) / 2, nt = packed_b_tiles(N);
+  if (kw == 0 || nt == 0) return cudaSuccess;
+  dim3 grid((unsigned)kw, (unsigned)nt);
+  dev::pack_b_sw64_kernel<<<grid, 128, 0, s>>>(packed32, out, kbs, kw);
+  return cudaGetLastError();
+}
 
 int64_t packed_b_tiles(int64_t N) {
   const int64_t t = (N + 127) / 128;

@@ -25,6 +25,13 @@ size_t packed_b_bytes(int64_t K, int64_t N);
 cudaError_t pack_b(const void* in, int in_dtype, int layout, int64_t ldi, int out_mode, uint8_t* out,
                    int64_t K, int64_t N, const int32_t* kperm, cudaStream_t s);
 
+// The 2:4 path's copy of B: 8 KB tiles ordered [128-column tile][window],
+// window w = k-blocks 2w and 2w+1 (32 k-values; the second half zero past
+// K), 128 rows of 64 bytes in the 64-byte swizzle, made from the packed
+// FP16/BF16 tiles of pack_b.
+size_t packed_b64_bytes(int64_t K, int64_t N);
+cudaError_t pack_b_sw64(const uint8_t* packed32, int64_t K, int64_t N, uint8_t* out, cudaStream_t s);
+
 // One B operand of a grouped pack: tiles of `in` (in_dtype, layout, ldi,
 // K x N) into `out` (out_mode as pack_b), covering global blocks
 // [begin, begin + ntiles * ceil(K / 16)).

@@ -46,8 +46,8 @@ namespace {
 
 // (device, M, K, block count, block width, then address and buffer ID of
 // each array: values, row pointers, column starts, and the same three of the
-// dense part for the separate variant)
-using Key = std::tuple<int, size_t, size_t, size_t, int, std::array<uint64_t, 12>>;
+// dense part and the relative block index map for the separate variant)
+using Key = std::tuple<int, size_t, size_t, size_t, int, std::array<uint64_t, 14>>;
 
 struct Entry {
   smat_bcsr* h = nullptr;
@@ -70,7 +70,7 @@ uint64_t buffer_id(const void* p) {
 }
 
 Key make_key(int dev, size_t M, size_t K, size_t nnzb, int bw, std::initializer_list<const void*> arrays) {
-  std::array<uint64_t, 12> a{};
+  std::array<uint64_t, 14> a{};
   size_t i = 0;
   for (const void* p : arrays) {
     a[i++] = (uint64_t)(uintptr_t)p;
@@ -148,15 +148,21 @@ void run(const half* vals, const int* rowptr, const int* colidx, const half* B, 
 
 // Merges two BCSRs with the same block shape (the 2:4 part and the dense part
 // of filterBcsrBlocks, matrix.h:1140-1288) into one, per block row in column
-// order, and runs it.
+// order, and runs it. Where a block's values are: with a relative block
+// index map (the reference harness, tester.h:554-590, passes the full BCSR's
+// values for both parts and its map), block (r, c) is at
+// vs[rel[r * K/bw + c/bw]], as the reference kernel reads it
+// (mmaOBTS_large_separate.cu:156-186); without one (rel == nullptr), each
+// part's k-th block is at its own values array's k-th block.
 void run_separate(const half* vs, const int* rps, const int* cis, const half* vd, const int* rpd, const int* cid,
-                  const half* B, half* C, size_t M, size_t N, size_t K, int bw) {
+                  const half* B, half* C, size_t M, size_t N, size_t K, size_t nnzb_full, const int* rel, int bw) {
   smat_status st = SMAT_OK;
   int dev = 0;
   cudaGetDevice(&dev);
-  // the merged matrix is keyed on both parts' arrays (block count 0: the
-  // parts' counts are in their row pointers)
-  const Key key = make_key(dev, M, K, 0, bw, {vs, rps, cis, vd, rpd, cid});
+  // the merged matrix is keyed on both parts' arrays and the map (block
+  // count: the full BCSR's with a map, else 0: the parts' counts are in
+  // their row pointers)
+  const Key key = make_key(dev, M, K, rel ? nnzb_full : 0, bw, {vs, rps, cis, vd, rpd, cid, rel});
   Entry* e = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);
@@ -171,20 +177,33 @@ void run_separate(const half* vs, const int* rps, const int* cis, const half* vd
     const half* vp[2] = {vs, vd};
     std::vector<int32_t> ci[2];
     std::vector<uint16_t> v[2];
+    std::vector<int32_t> relh;  // the relative block index map, when given
+    const size_t ncb = bw > 0 ? K / (size_t)bw : 0;
+    if (M % 16 || K % bw) st = smat::fail(SMAT_ERR_INVALID, "M and K must be multiples of the block shape");
+    if (st == SMAT_OK && rel) {
+      // with a map both parts read the first values array (the full BCSR)
+      relh.resize(nbr * ncb);
+      v[0].resize(nnzb_full * bsz);
+      if ((!relh.empty() &&
+           cudaMemcpy(relh.data(), rel, relh.size() * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) ||
+          (nnzb_full &&
+           cudaMemcpy(v[0].data(), vs, v[0].size() * sizeof(uint16_t), cudaMemcpyDeviceToHost) != cudaSuccess))
+        st = smat::fail(SMAT_ERR_CUDA, "copying the block map or values failed");
+    }
     for (int p = 0; p < 2 && st == SMAT_OK; p++) {
-      if (M % 16 || K % bw) {
-        st = smat::fail(SMAT_ERR_INVALID, "M and K must be multiples of the block shape");
-        break;
-      }
       if (cudaMemcpy(rp[p].data(), rpp[p], (nbr + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) {
         st = smat::fail(SMAT_ERR_CUDA, "copying row pointers failed");
         break;
       }
       const size_t nb = (size_t)rp[p][nbr];
       ci[p].resize(nb);
+      if (nb && cudaMemcpy(ci[p].data(), cip[p], nb * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        st = smat::fail(SMAT_ERR_CUDA, "copying BCSR arrays failed");
+        break;
+      }
+      if (rel) continue;
       v[p].resize(nb * bsz);
-      if (nb && (cudaMemcpy(ci[p].data(), cip[p], nb * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
-                 cudaMemcpy(v[p].data(), vp[p], nb * bsz * sizeof(uint16_t), cudaMemcpyDeviceToHost) != cudaSuccess))
+      if (nb && cudaMemcpy(v[p].data(), vp[p], nb * bsz * sizeof(uint16_t), cudaMemcpyDeviceToHost) != cudaSuccess)
         st = smat::fail(SMAT_ERR_CUDA, "copying BCSR arrays failed");
     }
     if (st == SMAT_OK) {
@@ -201,7 +220,19 @@ void run_separate(const half* vs, const int* rps, const int* cis, const half* vd
             break;
           }
           mci.push_back(ci[p][k]);
-          mv.insert(mv.end(), v[p].begin() + (size_t)k * bsz, v[p].begin() + (size_t)(k + 1) * bsz);
+          size_t src = (size_t)k;  // block index in the values array it comes from
+          const std::vector<uint16_t>* vv = &v[p];
+          if (rel) {
+            const int64_t col = ci[p][k];
+            const int64_t ri = col >= 0 && (size_t)col < K ? relh[r * ncb + (size_t)col / bw] : -1;
+            if (ri < 0 || (size_t)ri >= nnzb_full) {
+              st = smat::fail(SMAT_ERR_INVALID, "a block of a part is not in the relative block index map");
+              break;
+            }
+            src = (size_t)ri;
+            vv = &v[0];
+          }
+          mv.insert(mv.end(), vv->begin() + src * bsz, vv->begin() + (src + 1) * bsz);
         }
         mrp[r + 1] = (int32_t)mci.size();
         if (st != SMAT_OK) break;
@@ -272,11 +303,9 @@ void mmaOBTSKernel_large_separate(half* bcsrValuesA_sparse, int* bcsrRowPtrA_spa
                                   size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping) {
   (void)metadata;
   (void)sparseMatrixA;
-  (void)nonzeroBlocks;
   (void)blockInfo;
-  (void)relativeBlockIndexMapping;
   run_separate(bcsrValuesA_sparse, bcsrRowPtrA_sparse, bcsrColIdxA_sparse, bcsrValuesA_dense, bcsrRowPtrA_dense,
-               bcsrColIdxA_dense, B, C, M, N, K, 32);
+               bcsrColIdxA_dense, B, C, M, N, K, nonzeroBlocks, relativeBlockIndexMapping, 32);
 }
 
 // ---------------------------------------------------------------- C helpers

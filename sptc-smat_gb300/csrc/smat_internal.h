@@ -1,12 +1,14 @@
 // smat_internal.h — shared declarations of libsmat's host side.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "smat.h"
+#include "spmm24.h"
 #include "spmm_tc.h"
 
 namespace smat {
@@ -87,7 +89,23 @@ struct Plan {
   int64_t n_tiles = 0;               // B tile loads per pass over A
 };
 
-smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan);
+// skip (optional): blocks with skip[k] != 0 are left out of the plan (the
+// exact-2:4 blocks that the structured-sparse path computes).
+smat_status build_plan(const HostBcsr& b, int32_t R, int32_t cls, Plan& plan,
+                       const std::vector<uint8_t>* skip = nullptr);
+
+// ------------------------------------------------------------------ 2:4 path
+// The structured-sparse path's units, stages and groups (spmm24.h) and the
+// compressed stream, for the blocks with take[k] != 0 (16 x 16 blocks, all
+// exactly 2:4); fmt 0: FP16 values, 1: BF16.
+struct Sp24Host {
+  std::vector<uint8_t> stream;
+  std::vector<Sp24Stage> stages;
+  std::vector<Sp24Group> groups;     // heaviest first
+  std::vector<int32_t> unit_window;
+  int64_t n_blocks = 0, n_units = 0;
+};
+smat_status build_sp24(const HostBcsr& b, const std::vector<uint8_t>& take, int fmt, Sp24Host& out);
 
 // The reference's per-block sparsity label (csrToBcsr, matrix.h:679-711), per
 // BCSR block: 1 = "2:4" (the default), 2 = dense once a row of the block has
@@ -139,6 +157,16 @@ struct SmatBcsrBody {
   uint32_t forms = 0;
   int use24 = 0;
   int64_t n_24 = 0;
+  // 2:4 path (use24 and 16 x 16 blocks): the groups, stages and unit windows
+  // (shared by the forms) and one compressed stream per form (FP16, BF16)
+  int sp24_on = 0;
+  int32_t sp24_ngroups = 0;
+  int64_t sp24_units = 0;
+  Sp24Stage* d_sp24_stages = nullptr;
+  Sp24Group* d_sp24_groups = nullptr;
+  int32_t* d_sp24_unit_window = nullptr;
+  uint8_t* d_sp24_stream[2] = {nullptr, nullptr};
+  int32_t* d_bcsr_row_map = nullptr;  // [rows_padded] BCSR row -> C row
   int num_sms = 0;
   int32_t* d_kperm = nullptr;  // column permutation for the B gather (or null)
   // A stream per form (F16, BF16, -, SPLIT): per stage the pre-swizzled
@@ -149,6 +177,8 @@ struct SmatBcsrBody {
   std::vector<uint8_t> fp8_q;
   std::vector<float> fp8_scale;
   int* d_err = nullptr;
+  uint64_t wait_ns = 0;              // device-side wait limit (0: the kernels' default)
+  std::atomic<int32_t> stall{0};     // testing hook: one-shot stall stage of the next launch
   // smat_spmm_host staging
   std::mutex mu;
   void* d_bstage = nullptr;
@@ -182,11 +212,13 @@ constexpr double kDefaultSplitFrac = 0.5;
 int pick_nsub(const smat_bcsr* h, int64_t N, int kind);
 
 // Workspace layout of one SpMM: [packed B (x2 for the split form)]
+// [the 2:4 path's copy of B, when the handle uses it for this form]
 // [the launch's next-item counter, 16 bytes]
 // [per split panel, column tile and TMEM lane quadrant: an int counter]
 // [per part of a split panel and column tile: an R*bh x BN FP32 slab].
 struct WsLayout {
   size_t counters = 0, counter_bytes = 0, slabs = 0, total = 0;
+  size_t b64 = 0;  // the 2:4 path's copy of B (0: none)
 };
 WsLayout ws_layout(const smat_bcsr* A, int32_t form, int64_t N);
 

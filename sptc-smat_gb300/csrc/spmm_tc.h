@@ -65,7 +65,7 @@ __host__ __device__ constexpr int fp8_scale_bytes(int n) { return (4 * n + 15) /
 // Stage header (little-endian), kStageHdrFixed bytes then one 32-bit entry
 // per MMA group, grouped by issuing warp:
 //   uint16 warp_list[4]   bits 0-7 first entry of warp w, bits 8-15 its entry count
-//   uint16 nblk, pad[3]
+//   uint16 nblk, ntiles, pad[2]
 //   uint32 entry[...]
 // A group is a run of consecutive block rows ("slots") with a block at the
 // same block column, the same accumulate flag and the same owner; it is one
@@ -121,6 +121,9 @@ struct ProblemDesc {
 // then order[grid + atomicAdd(next_item, 1)], ... until the list is done:
 // the items are sorted by decreasing estimated cost, so whichever CTA is
 // free first takes the largest item left (the counter is zero at launch).
+// wait_ns bounds every device-side wait (0: 4 s); stall_stage k > 0 makes
+// the first MMA-issuing thread of CTA 0 wait, before its k-th stage, on a
+// barrier nothing arrives at (a test of the bounded-wait error path).
 struct SpmmArgs {
   ProblemDesc one;
   const ProblemDesc* probs;
@@ -129,7 +132,8 @@ struct SpmmArgs {
   const WorkItem* items;
   int* err;
   int32_t n_items;
-  int32_t pad_;
+  int32_t stall_stage;
+  uint64_t wait_ns;
 };
 
 // Kernel kinds: 0 plain (FP16 or BF16 A and B), 1 split hi+lo BF16, 2 FP8 A

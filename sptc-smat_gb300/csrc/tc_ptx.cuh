@@ -10,7 +10,8 @@
 namespace smat {
 namespace dev {
 
-// A bounded wait gives up after this long (ns) and reports SMAT_ERR_TIMEOUT.
+// A bounded wait gives up after this long (ns, unless the launch passes a
+// limit of its own) and reports SMAT_ERR_TIMEOUT.
 constexpr uint64_t kWaitTimeoutNs = 4000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -48,17 +49,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Wait for the phase with the given parity to complete. Gives up when the
-// CTA's abort flag is raised or after kWaitTimeoutNs; in the latter case it
-// raises the abort flag and records `where` in the global error word.
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
-                                       int where) {
+// CTA's abort flag is raised or after `lim` ns; in the latter case it raises
+// the abort flag and records `where` in the global error word.
+static __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
+                                       int where, uint64_t lim) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 31u) == 0) {
       if (*abort) return false;
-      if (globaltimer() - t0 > kWaitTimeoutNs) {
+      if (globaltimer() - t0 > lim) {
         *abort = 1;
         atomicCAS(err, 0, where);
         return false;
@@ -70,8 +71,8 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile i
 // mbar_wait for waits expected to be long (a whole panel): after a few
 // polls the thread sleeps between them so that it leaves the issue slots of
 // its SM sub-partition to the warps on the critical path.
-__device__ __noinline__ bool mbar_wait_sleepy(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
-                                              int where) {
+static __device__ __noinline__ bool mbar_wait_sleepy(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
+                                              int where, uint64_t lim) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 1;; ++it) {
@@ -79,7 +80,7 @@ __device__ __noinline__ bool mbar_wait_sleepy(uint32_t bar, uint32_t parity, vol
     if (it > 4) __nanosleep(256);
     if ((it & 7u) == 0) {
       if (*abort) return false;
-      if (globaltimer() - t0 > kWaitTimeoutNs) {
+      if (globaltimer() - t0 > lim) {
         *abort = 1;
         atomicCAS(err, 0, where);
         return false;

@@ -286,6 +286,14 @@ class Bcsr:
         return (rp, ci[:n], vals[: n * i["block_rows"] * i["block_cols"]].view(np.float16)
                 .reshape(n, i["block_rows"], i["block_cols"]), is24[:n])
 
+    def set_wait_limit(self, ns: int):
+        """Limit of every device-side wait of this matrix's SpMMs (0: 4 s)."""
+        check(lib().smat_bcsr_set_wait_limit(self._h, int(ns)))
+
+    def debug_stall(self, stage: int):
+        """Testing hook: the next SpMM stalls before the given stage until its wait limit."""
+        check(lib().smat_bcsr_debug_stall(self._h, int(stage)))
+
     def workspace_size(self, form: int, b_dtype: int, N: int) -> int:
         n = C.c_size_t()
         check(lib().smat_spmm_workspace_size(self._h, form, b_dtype, N, C.byref(n)))

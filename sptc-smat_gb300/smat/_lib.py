@@ -112,6 +112,8 @@ _SIGS = {
     "smat_spmm_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                                  C.c_int32, C.c_int64, C.c_int64, C.c_void_p]),
     "smat_bcsr_check_device_error": (C.c_int, [C.c_void_p]),
+    "smat_bcsr_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "smat_bcsr_debug_stall": (C.c_int, [C.c_void_p, C.c_int32]),
     "smat_ref_shims_last_status": (C.c_int, []),
     "smat_ref_shims_release": (C.c_int, []),
     "smat_last_error": (C.c_char_p, []),
@@ -173,6 +175,8 @@ REF_SHIMS = {
                                       _IP, _IP]),
     "preprocessing_mmaSTKernel": ("_Z25preprocessing_mmaSTKernelP6__halfPcS0_mmmmPiS2_",
                                   [_HP, C.c_void_p, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+    "preprocessing_mmaSTKernel_large": ("_Z31preprocessing_mmaSTKernel_largeP6__halfPcS0_mmmmPiS2_",
+                                        [_HP, C.c_void_p, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
 }
 
 
