@@ -355,6 +355,54 @@ def run_smat(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms, kern_ms = float(t[0]), float(t[1])
 
+    # the same step with the structured-sparse path on: exact-2:4 blocks on
+    # tcgen05.mma.sp (second launch), the others on the dense kernel
+    sp24 = None
+    if not args.no_sp24:
+        M24 = smat.Bcsr(A, block=(16, 16), forms=(smat.FORM_F16,), row_perm=perm, device=local, use_24=True)
+        ws24_bytes = M24.workspace_size(smat.FORM_F16, smat.F16, N)
+        ws24 = torch.empty(ws24_bytes, dtype=torch.uint8, device=dev)
+        C24 = torch.empty((A.rows, N), dtype=torch.float32, device=dev)
+
+        def step24():
+            M24.spmm_raw(smat.FORM_F16, B, smat.F16, smat.COL_MAJOR, A.cols, C24, smat.F32, N, N, ws24, ws24_bytes, sp)
+
+        step24()
+        torch.cuda.synchronize(dev)
+        M24.check_device_error()
+        got24 = C24.cpu().numpy().astype(np.float64)
+        ref = Asp @ Bh.astype(np.float64)
+        err24 = float(np.linalg.norm(got24 - ref) / np.linalg.norm(ref))
+        del ref, got24
+        for _ in range(max(args.warmup, 3)):
+            step24()
+        g24 = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g24, stream=stream):
+            step24()
+        with torch.cuda.stream(stream):
+            g24.replay()
+        torch.cuda.synchronize(dev)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            f0.record(stream)
+            for _ in range(args.steps):
+                g24.replay()
+            f1.record(stream)
+        torch.cuda.synchronize(dev)
+        M24.check_device_error()
+        ms24 = f0.elapsed_time(f1) / args.steps
+        i24 = M24.info
+        # 2:4 blocks move 256 B of kept values + 32 B of metadata instead of 512 B
+        n24 = i24["n_blocks_24"]
+        sp24 = {"value": world * 2.0 * A.nnz * N / (ms24 * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms24,
+                "n_blocks_24": n24, "nnzb": i24["nnzb"], "rel_err_vs_fp64": err24,
+                "a_bytes": (i24["nnzb"] - n24) * 512 + n24 * 288, "a_bytes_dense_path": i24["nnzb"] * 512,
+                "step": "pack B (4 KB tiles, then 8 KB 2:4 windows) + dense SpMM over the other blocks + "
+                        "tcgen05.mma.sp over the exact-2:4 blocks (4 launches), one CUDA graph"}
+        log(f"[bench] 2:4 path: {n24} of {i24['nnzb']} blocks on mma.sp, {ms24:.4f} ms/step, rel err {err24:.3e}")
+        M24.close()
+        del ws24, C24
+
     # e2e through the host-buffer entry point: pinned B in, C out, every step
     Bhost = torch.empty((N, A.cols), dtype=torch.float16).pin_memory()
     Bhost.copy_(torch.from_numpy(np.ascontiguousarray(Bh.T)))
@@ -412,6 +460,8 @@ def run_smat(args):
                 "h2d_bytes_per_step": A.cols * N * 2, "d2h_bytes_per_step": A.rows * N * 4, "ms_per_step": e2e_ms},
         "gpu_launches": 2 * args.steps,
     }
+    if sp24 is not None:
+        line["sp24_path"] = sp24
     if rank == 0:
         cpu_v, sample = cpu_baseline(A, N, threads=1, budget_s=12.0)
         line["cpu_baseline"] = {"value": cpu_v, "unit": "TFLOP/s", "cores": 1, "kind": "port",
@@ -624,6 +674,7 @@ def main():
                          "headline inputs, for comparison; rmat16_reorder: the reorder step alone "
                          "(with --impl reference: the reference's own reorder)")
     ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--no-sp24", action="store_true", help="skip the structured-sparse (2:4) path's line")
     args = ap.parse_args()
     if args.workload == "rmat16_reorder":
         run_reorder(args)

@@ -12,7 +12,9 @@
 // Roles (384 threads), one CTA per SM, groups taken round-robin from a list
 // sorted by decreasing work:
 //   warp 0        MMA issuer (lane 0); owns TMEM (two 128-column
-//                 accumulators, then one metadata column per A-tile slot).
+//                 accumulators, then the metadata column of each A-tile
+//                 slot, 64 columns apart: the MMA's metadata address is
+//                 kept on a 64-column boundary).
 //   warp 1        stage copies: the compact unit data (values, metadata).
 //   warp 2        B copies: one 8 KB tile (32 rows of B x 128 columns,
 //                 64-byte swizzle) per unit.
@@ -60,10 +62,13 @@ struct Sp24Cfg {
   static constexpr uint32_t RING = OFF_B + NBT * BTILE;
   static constexpr uint32_t NBARS = 2 * NS + 2 * NT + 2 * NBT + 4 + 1;
   static constexpr uint32_t SMEM_BYTES = 1024 + RING + 8 * NBARS + 16;
+  static constexpr uint32_t META_COL0 = 256;                     // metadata column of A slot t: META_COL0 + 64 t
+  static constexpr uint32_t META_STRIDE = 64;
   static constexpr uint32_t TMEM_COLS = 512;                     // 2 x 128 accumulator + NT metadata
   static constexpr int THREADS = 384;
   static_assert(STAGE_MAX % 16 == 0, "stage bytes");
   static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+  static_assert(META_COL0 + META_STRIDE * (NT - 1) < TMEM_COLS, "metadata columns inside the allocation");
 };
 
 __device__ __forceinline__ bool w24(uint32_t bar, uint32_t parity, volatile int* abort, int* err, int where,
@@ -241,7 +246,7 @@ __global__ void __launch_bounds__(Sp24Cfg::THREADS, 1) spmm24_kernel(const __gri
             tc_fence_after();
             const uint64_t ad = desc_kmajor_sw32(smem0 + C::OFF_A + t * C::ATILE);
             const uint64_t bd = desc_kmajor_sw64(smem0 + C::OFF_B + x * C::BTILE);
-            umma_sp_f16(tmem + buf * 128, ad, bd, tmem + 256 + t, args.idesc | ((128u >> 3) << 17), i > 0 ? 1u : 0u);
+            umma_sp_f16(tmem + buf * 128, ad, bd, tmem + C::META_COL0 + C::META_STRIDE * t, args.idesc | ((128u >> 3) << 17), i > 0 ? 1u : 0u);
             issued = true;
             umma_commit(smem_u32(&a_free[t]));
             umma_commit(smem_u32(&b_free[x]));
@@ -260,10 +265,12 @@ __global__ void __launch_bounds__(Sp24Cfg::THREADS, 1) spmm24_kernel(const __gri
     // Thread r (0..127) owns row r of every unit: block row j = r / 16 of the
     // group, row r % 16 of its blocks. It writes the row's 32 bytes of the A
     // tile (16 kept values: the window's first half, then its second; zeros
-    // where the block row has no 2:4 block) in the 32-byte swizzle, and the
-    // row's metadata word (first half's 16 bits low, second half's high;
-    // 0x4444 for an absent half: indices 0 and 1 of zero values) into the
-    // unit's TMEM column.
+    // where the block row has no 2:4 block) in the 32-byte swizzle, and TMEM
+    // lane r of the unit's metadata column. The sparse MMA reads metadata per
+    // 16-row slab (here: one block row j): lane 16 j + 8 h + i holds the
+    // 16-bit metadata of K-half h (the window's block h) for row i of the
+    // slab in bits 0..15 and for row i + 8 in bits 16..31 (0x4444 for an
+    // absent block: indices 0 and 1 of zero values).
     const int q = warp - 8;
     const int r = q * 32 + lane;
     const int j = r >> 4, rr = r & 15;
@@ -293,22 +300,28 @@ __global__ void __launch_bounds__(Sp24Cfg::THREADS, 1) spmm24_kernel(const __gri
             }
             const uint32_t mask = units[i].mask;
             const uint32_t first = units[i].first;
-            uint32_t word = 0;
             uint8_t* arow = smem + C::OFF_A + t * C::ATILE + r * 32;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
               const uint32_t bit = 2u * j + h;
               uint4 v = make_uint4(0, 0, 0, 0);
-              uint32_t m16 = 0x4444u;
               if ((mask >> bit) & 1u) {
                 const uint32_t blk = first + __popc(mask & ((1u << bit) - 1u));
                 v = *reinterpret_cast<const uint4*>(vals + (size_t)blk * 256 + rr * 16);
-                m16 = *reinterpret_cast<const uint16_t*>(metas + (size_t)blk * 32 + rr * 2);
               }
               *reinterpret_cast<uint4*>(arow + ((h ^ ((r >> 2) & 1)) << 4)) = v;
-              word |= m16 << (16 * h);
             }
-            tmem_st_x1(tmem + ((uint32_t)(q * 32) << 16) + 256 + t, word);
+            uint32_t word = 0x44444444u;
+            {
+              const uint32_t mh = (r >> 3) & 1u, mi = r & 7u;  // K-half and slab row of this lane
+              const uint32_t bit = 2u * j + mh;
+              if ((mask >> bit) & 1u) {
+                const uint32_t blk = first + __popc(mask & ((1u << bit) - 1u));
+                const uint16_t* mp = reinterpret_cast<const uint16_t*>(metas + (size_t)blk * 32);
+                word = (uint32_t)mp[mi] | ((uint32_t)mp[mi + 8] << 16);
+              }
+            }
+            tmem_st_x1(tmem + ((uint32_t)(q * 32) << 16) + C::META_COL0 + C::META_STRIDE * t, word);
             tmem_st_wait();
             fence_proxy_async_smem();
             tc_fence_before();

@@ -15,42 +15,31 @@
 // B tile of a column is loaded once and used by every block row of the panel
 // that has a block there. The A blocks are stored on the device in exactly
 // that visiting order, already in the shared-memory layout the MMA reads
-// (32-byte swizzle), cut into STAGES: a stage is up to 28 A blocks (14 of 32
-// rows) with the stage's MMA list (precomputed on the host, stored after the
-// blocks so that one copy brings both) and up to 14 B tiles.
+// (32-byte swizzle). The pipeline moves STAGES: one stage carries up to 16
+// A blocks (8 of 32 rows), up to 8 packed B tiles those blocks need and the
+// stage's MMA list (precomputed on the host, stored after the stage's A
+// blocks so that one copy brings both), so the hand-off between the copy
+// engine and the tensor cores is one full/empty barrier pair per stage.
 //
-// The two operands move through separate rings in shared memory, because
-// they come from different places: the A blocks stream from HBM once (long
-// latency, ~14 KB per stage) into a ring of NA stage slots that runs several
-// stages ahead; the B tiles come from L2 (B is small and re-read by many
-// panels) into a ring of NB single-tile slots, filled tile by tile in
-// consumption order, so that a stage's tiles occupy whatever slots the
-// stages before it freed. One "stage done" barrier per stage, to which every
-// MMA-issuing warp commits, frees the stage's A slot and its B slots.
-//
-// Roles (512 threads; 640 for the FP8 form):
-//   warp 8          A copies: lane 0 takes the CTA's work items (the launch's
-//                   counter) into a small item ring for the other roles, and
-//                   issues one bulk copy per stage (A blocks + MMA list).
-//   warps 9..15     B copies: tile j of stage c goes to warp (j + c) mod 7;
-//                   lane 0 of warp 9 waits until the stage's ring slots are
-//                   free and passes the verdict on through a named barrier.
+// Roles (512 threads):
+//   warps 8..15     copy warps: a stage needs one bulk copy for its A blocks
+//                   and list and one per B tile; the copies rotate over the
+//                   eight warps (a warp keeps only about one copy at a time
+//                   in flight).
 //   warps 0..3      MMA issuers, lane 0 each, one per quarter of the panel's
-//                   block rows (one thread issues at most one narrow
-//                   tcgen05.mma per ~80-150 cycles; four keep the tensor pipe
-//                   near its rate); warp 0 also owns TMEM.
+//                   block rows (one thread issues at most one tcgen05.mma
+//                   per ~80-150 cycles; four keep the tensor pipe at its
+//                   per-instruction rate); warp 0 also owns TMEM.
 //   warps 4..7      epilogue: tcgen05.ld -> row scatter through row_map ->
 //                   FP32 or FP16 stores of C (coalesced along N).
-//   warps 16..19    FP8 form only: e4m3 -> FP16 conversion of each stage's
-//                   A blocks in shared memory.
 //
 // Consecutive block rows with a block at the same column form one MMA
 // (N = bh * run length), so dense panels need far fewer instructions.
 //
-// Every wait is bounded (see tc_ptx.cuh; the launch may pass its own limit);
-// on a timeout the kernel raises the CTA's abort flag, records the site in
-// the global error word, lets the producers wait for their own copies in
-// flight and the MMA threads for their own MMAs, frees TMEM and returns.
+// Every wait is bounded (see tc_ptx.cuh); on a timeout the kernel raises the
+// CTA's abort flag, records the site in the global error word, lets the
+// producers wait for their own copies in flight and the MMA threads for
+// their own MMAs, frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -79,15 +68,14 @@ enum : int {
   ERR_EPI = 301,
   ERR_CONV = 302,
   ERR_DRAIN = 401,
-  ERR_ITEM_TAKE = 103,  // the A copy warp waited for a free item-ring slot
-  ERR_ITEM_B = 104,     // the B copy leader waited for its next item
+  ERR_ITEM_TAKE = 103,  // the copy warps waited for a free item-ring slot
   ERR_ITEM_MMA = 204,   // an MMA warp waited for its next item
   ERR_ITEM_EPI = 303,
   ERR_ITEM_CONV = 304
 };
 
-// Entries of the CTA's ring of work items (the A copy warp takes items from
-// the launch's counter and runs up to a few items ahead of the other roles).
+// Entries of the CTA's ring of work items (the copy warps take items from
+// the launch's counter and run up to a few items ahead of the other roles).
 constexpr int kItemRing = 4;
 
 template <int BH, int R, int NSUB, int KIND>
@@ -97,53 +85,43 @@ struct Cfg {
   static constexpr int CLS = KIND == KIND_SPLIT ? 1 : (KIND == KIND_FP8 ? 2 : 0);  // plan class (stage shape)
   static constexpr int SB = stage_rows(CLS) / BH;         // A blocks per stage (at most)
   static constexpr int ST = stage_tiles(CLS);             // B tiles per stage (at most)
-  static constexpr int HDRMAX = (stage_hdr_max(SB) + 15) / 16 * 16;  // the header is copied in 16-byte units
+  static constexpr int HDRMAX = stage_hdr_max(SB);
   static constexpr uint32_t ABLK = BH * 32;               // bytes of one A block (one operand)
   static constexpr uint32_t TILE = BN * 32;               // bytes of one B tile (one operand)
-  static constexpr uint32_t TILEB = TILE * NOPS;          // bytes of one B ring slot
+  static constexpr uint32_t TILEB = TILE * NOPS;          // bytes of one B tile slot
   static constexpr bool FP8 = KIND == KIND_FP8;
-  // A slot: [A blocks hi | lo | header]; the FP8 form lands [e4m3 blocks |
-  // scales | header] in a staging area after the A blocks, which the
-  // converter warps turn into FP16 A blocks
+  // stage: [A blocks hi | lo | header] [B tiles] [header offset word]; the
+  // FP8 form lands [e4m3 blocks | scales | header] in a staging area after
+  // the A blocks, which the converter warps turn into FP16 A blocks
   static constexpr uint32_t OFF_STG = SB * ABLK * NOPS;
   static constexpr uint32_t STG_BYTES = FP8 ? (SB * 256 + fp8_scale_bytes(SB) + HDRMAX + 255) / 256 * 256 : 0;
   static constexpr uint32_t A_END = FP8 ? OFF_STG + STG_BYTES : OFF_STG + HDRMAX;
-  static constexpr uint32_t ASLOT = (A_END + 255) / 256 * 256;   // operand tiles start on 256-byte boundaries
-  static constexpr int NA = 4;                                    // A stage slots
-  static constexpr uint32_t OFF_BR = (NA * ASLOT + 1023) / 1024 * 1024;  // B ring
-  static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
-  static constexpr int NPB = 7;                           // B copy warps (9..15)
-  static constexpr int NCONV = FP8 ? 4 : 0;               // FP8 converter warps (16..19)
-  static constexpr uint32_t SMEM_LIMIT = 227 * 1024;
-  static constexpr uint32_t BAR_RESERVE = 2048;           // barriers and small arrays (checked below)
-  static constexpr int NB_FIT = (int)((SMEM_LIMIT - 1024 - BAR_RESERVE - OFF_BR) / TILEB);
-  static constexpr int NB = NB_FIT > 48 ? 48 : NB_FIT;    // B tile slots
-  static constexpr int NSD = NB + 2;                      // stage-done barriers (> NB and > NA)
-  static constexpr uint32_t RING_BYTES = OFF_BR + NB * TILEB;
-  // barriers: a_full[NA], conv[NA] (FP8), b_full[NB], done[NSD], accfull[2],
-  // accempty[2], drain[NMMA], itemfull[ring], itemempty[ring], stall[1]
-  static constexpr uint32_t NBARS = NA + (FP8 ? NA : 0) + NB + NSD + 4 + NMMA + 2 * kItemRing + 1;
-  // then: the TMEM address, the abort flag, a_hw[NA], bq_start[NSD],
-  // item_ring[ring], the B copy warps' current item [2] and slot verdict [2]
-  static constexpr uint32_t NINTS = 2 + NA + NSD + kItemRing + 4;
-  static constexpr uint32_t SMEM_BYTES = 1024 + RING_BYTES + 8 * NBARS + 4 * NINTS;
+  static constexpr uint32_t OFF_B = (A_END + 1023) / 1024 * 1024;
+  static constexpr uint32_t OFF_HW = OFF_B + ST * TILEB;
+  static constexpr uint32_t STAGE = (OFF_HW + 16 + 1023) / 1024 * 1024;
+  static constexpr uint32_t SMEM_AVAIL = 227 * 1024 - 2048;  // minus alignment slack and barriers
+  static constexpr int NS_FIT = (int)(SMEM_AVAIL / STAGE);
+  static constexpr int NS = NS_FIT < 2 ? 2 : (NS_FIT > 8 ? 8 : NS_FIT);  // stages
   static constexpr uint32_t SUB_COLS = R * BH;            // TMEM columns of one 128-column subtile
   static constexpr uint32_t ACC_COLS = NSUB * SUB_COLS;   // TMEM columns per buffer
-  // accumulator buffers: two (the epilogue drains one while the MMAs fill
-  // the other) where they fit the 512 TMEM columns, else one (32-row panels)
-  static constexpr int NBUF = 2 * ACC_COLS <= 512 ? 2 : 1;
-  static constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;
-  static constexpr int THREADS = 32 * (9 + NPB + NCONV);  // MMA, epilogue, A copy, B copy, converter warps
+  static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
+  static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
+  static constexpr int NPROD = 8;                         // copy warps
+  static constexpr int NCONV = FP8 ? 4 : 0;               // FP8 converter warps (16..19)
+  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? NS : 0) + 2 * kItemRing + 1);
+  // then the TMEM address, the abort flag, stage_ok[NS], the item ring and
+  // the copy warps' current item
+  static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 8 + 4 * (NS + kItemRing + 1);
+  static constexpr int THREADS = 32 * (8 + NPROD + NCONV);  // MMA, epilogue, copy, converter warps
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
   static_assert(NSUB == 1, "packed B is [column tile][k-block]: a stage tile is one 128-column tile");
   static_assert(R <= 32, "slot field is 5 bits");
   static_assert(SB <= kMaxStageBlocks, "position field is 5 bits");
-  static_assert(ST <= 2 * NPB && ST <= kMaxStageTiles, "at most two B copies per copy warp and stage");
-  static_assert(NB >= ST, "a stage's B tiles must fit the ring");
-  static_assert(8 * NBARS + 4 * NINTS <= BAR_RESERVE, "barrier area");
-  static_assert(SMEM_BYTES <= SMEM_LIMIT, "shared memory per CTA");
+  static_assert(ST + 1 <= 2 * NPROD && ST <= kMaxStageTiles, "1 + ST copies per stage, at most two per copy warp");
+  static_assert(NS_FIT >= 2, "two stages must fit");
+  static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
   static_assert(!FP8 || (BH == 16 && NSUB == 1), "FP8 form: 16 x 16 blocks, 128-column tiles");
 };
 
@@ -202,6 +180,12 @@ __device__ __forceinline__ bool take_item_warp(uint64_t* itemfull, uint64_t* ite
   return got != 0;
 }
 
+// The copy index that copy warp pw issues first in stage c: copy j of a
+// stage goes to warp (j + c) mod nprod, so the duties rotate.
+__device__ __forceinline__ int copy_of(int pw, uint32_t c, int nprod) {
+  return (int)(((uint32_t)pw + (uint32_t)nprod - c % (uint32_t)nprod) % (uint32_t)nprod);
+}
+
 // Bounded wait for a whole warp: lane 0 polls, the warp learns the outcome
 // by shuffle and leaves converged (lanes that each polled would leave the
 // loop on different iterations and could run the code after it diverged).
@@ -224,7 +208,7 @@ __device__ __forceinline__ int64_t shfl_l(int64_t v, int src) {
 }
 
 // Warp roles: 0..3 MMA issuers (0 also owns TMEM), 4..7 epilogue (TMEM lane
-// quadrants 0..3), 8 A copies, 9..15 B copies, then (FP8) the converters.
+// quadrants 0..3), then NPROD copy warps, then (FP8) the converter warps.
 template <int BH, int R, int NSUB, int KIND>
 __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     spmm_tc_kernel(const __grid_constant__ SpmmArgs args) {
@@ -232,49 +216,41 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::RING_BYTES);
-  uint64_t* a_full = bars;                           // [NA] a stage's A copy landed
-  uint64_t* conv = a_full + C::NA;                   // [NA] (FP8) its A blocks are converted
-  uint64_t* b_full = conv + (C::FP8 ? C::NA : 0);    // [NB] a B tile landed
-  uint64_t* done = b_full + C::NB;                   // [NSD] a stage's MMAs completed (its slots are free)
-  uint64_t* accfull = done + C::NSD;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::NS * C::STAGE);
+  uint64_t* full = bars;
+  uint64_t* empty = full + C::NS;
+  uint64_t* accfull = empty + C::NS;
   uint64_t* accempty = accfull + 2;
   uint64_t* drainbar = accempty + 2;
-  uint64_t* itemfull = drainbar + C::NMMA;           // [kItemRing] an item index is in the ring
+  uint64_t* conv = drainbar + C::NMMA;  // FP8: the stage's A blocks are converted
+  uint64_t* itemfull = conv + (C::FP8 ? C::NS : 0);  // [kItemRing] an item index is in the ring
   uint64_t* itemempty = itemfull + kItemRing;        // [kItemRing] every role has read it
   uint64_t* stallbar = itemempty + kItemRing;        // nothing arrives here (test stall)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(stallbar + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  volatile int* a_hw = abort_flag + 1;               // [NA] header offset inside each A slot
-  volatile uint32_t* bq_start = reinterpret_cast<volatile uint32_t*>(a_hw + C::NA);  // [NSD] first tile of a stage
-  volatile int* item_ring = reinterpret_cast<volatile int*>(bq_start + C::NSD);      // [kItemRing]
-  // the B copy leader's item [by item parity] and verdict on a stage's slots
-  // [by stage parity], read by the B copy warps after a named barrier: the
-  // entry is written again only after the next barrier, which every warp
-  // reaches after reading it
-  volatile int* cur_item_b = item_ring + kItemRing;  // [2]
-  volatile int* b_ok = cur_item_b + 2;               // [2]
+  volatile int* stage_ok = abort_flag + 1;  // [NS]: the copy leader's verdict on the stage's slot
+  volatile int* item_ring = stage_ok + C::NS;     // [kItemRing] item indices (-1: no more work)
+  volatile int* cur_item = item_ring + kItemRing;  // the copy warps' current item
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t lim = args.wait_ns ? args.wait_ns : kWaitTimeoutNs;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < C::NA; i++) {
-      mbar_init(smem_u32(&a_full[i]), 1);  // the A copy warp's arrive (+ the copy's bytes)
-      if (C::FP8) mbar_init(smem_u32(&conv[i]), C::NCONV);
+    for (int i = 0; i < C::NS; i++) {
+      mbar_init(smem_u32(&full[i]), 1);  // the A copy warp's arrive (+ every copy's bytes)
+      mbar_init(smem_u32(&empty[i]), C::NMMA);
     }
-    for (int i = 0; i < C::NB; i++) mbar_init(smem_u32(&b_full[i]), 1);
-    for (int i = 0; i < C::NSD; i++) mbar_init(smem_u32(&done[i]), C::NMMA);
     for (int i = 0; i < 2; i++) {
       mbar_init(smem_u32(&accfull[i]), C::NMMA);
       mbar_init(smem_u32(&accempty[i]), 4);
     }
     for (int i = 0; i < C::NMMA; i++) mbar_init(smem_u32(&drainbar[i]), 1);
+    if (C::FP8)
+      for (int i = 0; i < C::NS; i++) mbar_init(smem_u32(&conv[i]), C::NCONV);
     for (int i = 0; i < kItemRing; i++) {
       mbar_init(smem_u32(&itemfull[i]), 1);
-      // lane 0 of every reader: MMA, epilogue, B copy leader, converters
-      mbar_init(smem_u32(&itemempty[i]), C::NMMA + 4 + 1 + C::NCONV);
+      mbar_init(smem_u32(&itemempty[i]), C::NMMA + 4 + C::NCONV);  // lane 0 of every other warp
     }
     mbar_init(smem_u32(stallbar), 1);
     *abort_flag = 0;
@@ -292,14 +268,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   int* err = args.err;
   const uint32_t smem0 = smem_u32(smem);
 
-  if (C::FP8 && warp >= 9 + C::NPB) {
+  if (C::FP8 && warp >= 8 + C::NPROD) {
     // ------------------------------------------------------ FP8 converters
-    // Each stage's e4m3 blocks and FP32 scales land in the staging area of
-    // its A slot; these four warps write them to the slot's A area as FP16
-    // (value times its block's scale, one rounding) in the 32-byte-swizzled
-    // layout the MMA reads, make the writes visible to the tensor core's
-    // async proxy, and release the stage to the MMA warps (conv barrier).
-    const int ct = threadIdx.x - 32 * (9 + C::NPB);
+    // Each stage's e4m3 blocks and FP32 scales land in the staging area;
+    // these four warps write them to the stage's A area as FP16 (value times
+    // its block's scale, one rounding) in the 32-byte-swizzled layout the
+    // MMA reads, make the writes visible to the tensor core's async proxy,
+    // and release the stage to the MMA warps (conv barrier).
+    const int ct = threadIdx.x - 32 * (8 + C::NPROD);
     uint32_t ci = 0;
     bool ok = true;
     for (uint32_t kk = 0; ok; ++kk) {
@@ -314,13 +290,13 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       const int n_tiles = P.n_tiles;
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
         for (int c = wi.s0; c < wi.s1; ++c, ++ci) {
-          const uint32_t s = ci % C::NA;
-          if (!warp_wait(smem_u32(&a_full[s]), (ci / C::NA) & 1, lane, abort_flag, err, ERR_CONV, false, lim)) {
+          const uint32_t s = ci % C::NS;
+          if (!warp_wait(smem_u32(&full[s]), (ci / C::NS) & 1, lane, abort_flag, err, ERR_CONV, false, lim)) {
             ok = false;
             break;
           }
-          uint8_t* stp = smem + s * C::ASLOT;
-          const uint32_t hw = (uint32_t)a_hw[s];
+          uint8_t* stp = smem + s * C::STAGE;
+          const uint32_t hw = *reinterpret_cast<const uint32_t*>(stp + C::OFF_HW);
           const int nblk = *reinterpret_cast<const uint16_t*>(stp + hw + 8);
           const uint8_t* stg = stp + C::OFF_STG;
           const float* scl = reinterpret_cast<const float*>(stg + nblk * 256);
@@ -345,124 +321,53 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
         }
       }
     }
-  } else if (warp == 8) {
-    // ------------------------------------------------------------- A copies
-    // Lane 0 takes the CTA's next work item from the launch's order (the
-    // CTA's own index first, then the shared counter) and puts it in the item
-    // ring for the other roles once they have read the entry it replaces.
-    // Then, stage by stage, once the stage NA earlier is done with its slot,
-    // it copies the stage's A region (blocks, FP8 scales, MMA list) into the
-    // slot with one bulk copy. Stage records are read 32 at a time, one per
-    // lane, and passed to lane 0 by shuffle.
+  } else if (warp >= 8) {
+    // ---------------------------------------------------------------- copies
+    // Stage number c (counted over the CTA's whole run) needs 1 + ntiles
+    // bulk copies: copy 0 = the A blocks and the MMA list, copy j = B tile
+    // j - 1. Copy warp p issues the copies j with (j + c) % NPROD == p (j and
+    // j + NPROD), so every warp issues one or two copies per stage and the A
+    // copy (from HBM, the slowest) rotates. A warp keeps only about one copy
+    // at a time in flight, so spreading them is what keeps the copy engine
+    // busy. The warp that
+    // issues copy 0 posts the stage's total byte count (arrive.expect_tx) on
+    // the stage's full barrier; the others only add their bytes as they land.
+    // Stage records are read 32 at a time, one per lane, and each lane
+    // prepares what its warp needs from its record.
+    const int pw = warp - 8;
     const uint64_t pol_a = make_l2_policy_evict_first();  // A streams through L2 once
+    const uint64_t pol_b = make_l2_policy_evict_last();   // B tiles are re-read by many CTAs
     uint32_t ci = 0;
     bool ok = true;
+    uint32_t last_mine = 0xffffffffu;  // last stage this warp copied into (for the drain)
     for (uint32_t kk = 0; ok; ++kk) {
-      int idx = -2;
-      if (lane == 0) {
+      // The CTA's next item: lane 0 of the first copy warp takes it from the
+      // launch's order (the CTA's own index first, then the shared
+      // counter), puts it in the item ring for the other roles once they
+      // have read the entry it replaces, and hands it to the copy warps.
+      if (pw == 0 && lane == 0) {
         const uint32_t r = kk % kItemRing;
+        int idx = -2;  // -2: aborted
         if (wait_phase(smem_u32(&itemempty[r]), ((kk / kItemRing) & 1) ^ 1, abort_flag, err, ERR_ITEM_TAKE, lim)) {
           const int pos = kk == 0 ? (int)blockIdx.x : (int)gridDim.x + atomicAdd(args.next_item, 1);
           idx = pos < args.n_items ? args.order[pos] : -1;
           item_ring[r] = idx;
           mbar_arrive(smem_u32(&itemfull[r]));
         }
+        *cur_item = idx;
       }
-      idx = shfl_i(idx, 0);
+      named_bar_sync(1, 32 * C::NPROD);
+      const int idx = *cur_item;
       if (idx < 0) {
         ok = idx == -1;
         break;
       }
       const WorkItem wi = args.items[idx];
       const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
+      // fields used after shared-memory stores, held in registers (the stores
+      // could alias P for the compiler and force a reload each time)
       const StageRec* const p_stages = P.stages;
       const uint8_t* const p_aval = P.aval;
-      const int n_tiles = P.n_tiles;
-      const int stage0 = P.panels[wi.panel].stage_off;
-      for (int nt = 0; nt < n_tiles && ok; ++nt) {
-        for (int base = wi.s0; base < wi.s1 && ok; base += 32) {
-          const int cnt = min(32, wi.s1 - base);
-          int64_t off = 0;
-          int bytes = 0, hword = 0;
-          if (lane < cnt) {
-            const StageRec* rp = p_stages + stage0 + base + lane;
-            const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
-            const int4 r1 = reinterpret_cast<const int4*>(rp)[1];           // nblk, hdr_bytes, ntiles, scl_off
-            if (C::FP8) {
-              off = r0.x * 256 + r1.w + r0.y;
-              bytes = r1.x * 256 + fp8_scale_bytes(r1.x) + r1.y;
-              hword = (int)C::OFF_STG + r1.x * 256 + fp8_scale_bytes(r1.x);
-            } else {
-              off = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
-              bytes = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
-              hword = r1.x * (int)(C::ABLK * C::NOPS);
-            }
-          }
-          for (int i = 0; i < cnt; ++i, ++ci) {
-            const int b1 = shfl_i(bytes, i);
-            const int hw = shfl_i(hword, i);
-            const int64_t o1 = shfl_l(off, i);
-            int good = 1;
-            if (lane == 0) {
-              const uint32_t s = ci % C::NA;
-              if (ci >= (uint32_t)C::NA) {
-                const uint32_t pc = ci - C::NA;  // the stage that used this slot before
-                good = wait_phase(smem_u32(&done[pc % C::NSD]), (pc / C::NSD) & 1, abort_flag, err, ERR_PROD_A, lim)
-                           ? 1
-                           : 0;
-              }
-              if (good) {
-                a_hw[s] = hw;
-                const uint32_t fb = smem_u32(&a_full[s]);
-                mbar_arrive_expect_tx(fb, (uint32_t)b1);
-                bulk_load_hint(smem0 + s * C::ASLOT + (C::FP8 ? C::OFF_STG : 0u), p_aval + o1, (uint32_t)b1, fb,
-                               pol_a);
-              }
-            }
-            if (!shfl_i(good, 0)) {
-              ok = false;
-              break;
-            }
-          }
-        }
-      }
-    }
-    if (!ok && lane == 0) {
-      // wait for the copies still in flight: only the last NA stages issued
-      // can have one
-      const uint32_t lo = ci > (uint32_t)C::NA ? ci - C::NA : 0;
-      for (uint32_t k = lo; k < ci; ++k) mbar_wait_drain(smem_u32(&a_full[k % C::NA]), (k / C::NA) & 1, err, lim);
-    }
-  } else if (warp >= 9) {
-    // ------------------------------------------------------------- B copies
-    // Tiles are numbered over the CTA's whole run (stage by stage, in the
-    // order the MMAs use them); tile t goes to ring slot t % NB. Before a
-    // stage's tiles are copied, lane 0 of warp 9 (the leader) waits until
-    // every stage whose tiles occupied those slots is done, and passes its
-    // verdict to the other copy warps through a named barrier. Tile j of
-    // stage c is copied by warp (j + c) mod NPB, so every warp issues one or
-    // two copies per stage and the duties rotate.
-    const int pw = warp - 9;
-    const bool leader = pw == 0 && lane == 0;
-    const uint64_t pol_b = make_l2_policy_evict_last();  // B tiles are re-read by many CTAs
-    uint32_t ci = 0, tb = 0, q_head = 0;  // stage count, tiles so far, oldest stage not known done
-    bool ok = true;
-    for (uint32_t kk = 0; ok; ++kk) {
-      if (leader) {
-        int idx = -1;
-        cur_item_b[kk & 1] = take_item_lane0(itemfull, itemempty, item_ring, kk, abort_flag, err, ERR_ITEM_B, lim, idx)
-                                 ? idx
-                                 : -2;
-      }
-      named_bar_sync(1, 32 * C::NPB);
-      const int idx = cur_item_b[kk & 1];
-      if (idx < 0) {
-        ok = idx == -1;
-        break;
-      }
-      const WorkItem wi = args.items[idx];
-      const ProblemDesc& P = args.probs ? args.probs[wi.prob] : args.one;
-      const StageRec* const p_stages = P.stages;
       const uint8_t* const p_bpack = P.bpack;
       const int64_t p_kbs = P.bp_kbs;
       const int n_tiles = P.n_tiles;
@@ -471,84 +376,107 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
         const int64_t bcol = (int64_t)nt * NSUB;  // first 128-column packed tile of this pass
         for (int base = wi.s0; base < wi.s1 && ok; base += 32) {
           const int cnt = min(32, wi.s1 - base);
-          // lane l prepares stage ci + l: its tile count and this warp's
-          // (at most two) tiles of it
+          // lane l prepares stage ci + l
           const uint32_t my_ci = ci + (uint32_t)lane;
-          const int j0 = (int)(((uint32_t)pw + (uint32_t)C::NPB - my_ci % (uint32_t)C::NPB) % (uint32_t)C::NPB);
-          int ntl = 0, kb1 = -1, kb2 = -1;
+          const int j0 = copy_of(pw, my_ci, C::NPROD);
+          int64_t off1 = 0, off2 = 0;
+          int bytes1 = 0, bytes2 = 0, dst1 = 0, dst2 = 0, total = 0, hword = 0;
           if (lane < cnt) {
             const StageRec* rp = p_stages + stage0 + base + lane;
-            ntl = rp->ntiles;
-            if (j0 < ntl) kb1 = rp->kb[j0];
-            if (j0 + C::NPB < ntl) kb2 = rp->kb[j0 + C::NPB];
+            const longlong2 r0 = reinterpret_cast<const longlong2*>(rp)[0];  // blk_off, hdr_off
+            const int4 r1 = reinterpret_cast<const int4*>(rp)[1];           // nblk, hdr_bytes, ntiles, -
+            const int ntl = r1.z;
+            if (j0 == 0) {
+              // the stage's A region (blocks, FP8 scales, header) in one copy
+              // (an L2 prefetch of it a few stages ahead measured slower:
+              // it competes with the copies for the copy engine)
+              if (C::FP8) {
+                off1 = r0.x * 256 + r1.w + r0.y;
+                bytes1 = r1.x * 256 + fp8_scale_bytes(r1.x) + r1.y;
+              } else {
+                off1 = r0.x * (int64_t)(C::ABLK * C::NOPS) + r0.y;
+                bytes1 = r1.x * (int)(C::ABLK * C::NOPS) + r1.y;
+              }
+              // header position inside the stage
+              hword = C::FP8 ? (int)C::OFF_STG + r1.x * 256 + fp8_scale_bytes(r1.x) : r1.x * (int)(C::ABLK * C::NOPS);
+              total = bytes1 + ntl * (int)C::TILEB;
+            }
+            // B copies, one per tile (several copies in flight land sooner
+            // than one long copy of adjacent tiles): copy j >= 1 brings tile
+            // j - 1, this warp's are tiles j0 - 1 and j0 + NPROD - 1
+            if (j0 >= 1 && j0 <= ntl) {
+              off1 = ((int64_t)bcol * p_kbs + rp->kb[j0 - 1]) * (4096 * C::NOPS);
+              bytes1 = (int)C::TILEB;
+              dst1 = j0 - 1;
+            }
+            if (j0 + C::NPROD <= ntl) {
+              off2 = ((int64_t)bcol * p_kbs + rp->kb[j0 + C::NPROD - 1]) * (4096 * C::NOPS);
+              bytes2 = (int)C::TILEB;
+              dst2 = j0 + C::NPROD - 1;
+            }
           }
           for (int i = 0; i < cnt; ++i, ++ci) {
-            const int n_t = shfl_i(ntl, i);
-            const int k1 = shfl_i(kb1, i);
-            const int k2 = shfl_i(kb2, i);
-            if (leader) {
-              // slots tb .. tb + n_t - 1 were last used by tiles tb - NB ..:
-              // every stage that started before tile tb + n_t - NB must be done
-              int good = 1;
-              while (q_head < ci && (int64_t)bq_start[q_head % C::NSD] < (int64_t)tb + n_t - C::NB) {
-                if (!wait_phase(smem_u32(&done[q_head % C::NSD]), (q_head / C::NSD) & 1, abort_flag, err, ERR_PROD_B,
-                                lim)) {
-                  good = 0;
-                  break;
+            const int b1 = shfl_i(bytes1, i);
+            const int b2 = shfl_i(bytes2, i);
+            const int d1 = shfl_i(dst1, i);
+            const int d2 = shfl_i(dst2, i);
+            const int64_t o1 = shfl_l(off1, i);
+            const int64_t o2 = shfl_l(off2, i);
+            const int tot = shfl_i(total, i);
+            const int hw = shfl_i(hword, i);
+            const int j = copy_of(pw, ci, C::NPROD);
+            const uint32_t s = ci % C::NS;
+            // The warp with copy 0 waits for the slot and passes its verdict
+            // to the other copy warps through a named barrier (blocked warps
+            // take no issue slots); so all copy warps move stage by stage and
+            // none can run a ring ahead and overwrite a stage still in use.
+            if (j == 0 && lane == 0)
+              stage_ok[s] = wait_phase(smem_u32(&empty[s]), ((ci / C::NS) & 1) ^ 1, abort_flag, err, ERR_PROD_A, lim) ? 1 : 0;
+            named_bar_sync(1, 32 * C::NPROD);
+            int good = 1;
+            if (lane == 0) {
+              if (stage_ok[s]) {
+                const uint32_t st = smem0 + s * C::STAGE;
+                const uint32_t fb = smem_u32(&full[s]);
+                if (b1 == 0) {
+                  // no copy for this warp in this stage
+                } else if (j == 0) {
+                  *reinterpret_cast<uint32_t*>(smem + s * C::STAGE + C::OFF_HW) = (uint32_t)hw;
+                  mbar_arrive_expect_tx(fb, (uint32_t)tot);
+                  bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), p_aval + o1, (uint32_t)b1, fb, pol_a);
+                } else {
+                  bulk_load_hint(st + C::OFF_B + d1 * C::TILEB, p_bpack + o1, (uint32_t)b1, fb, pol_b);
                 }
-                ++q_head;
+                if (b2 != 0) bulk_load_hint(st + C::OFF_B + d2 * C::TILEB, p_bpack + o2, (uint32_t)b2, fb, pol_b);
+                if (b1 != 0 || b2 != 0) last_mine = ci;
+              } else {
+                good = 0;
               }
-              bq_start[ci % C::NSD] = tb;
-              b_ok[ci & 1] = good;
             }
-            named_bar_sync(1, 32 * C::NPB);
-            if (!b_ok[ci & 1]) {
+            good = shfl_i(good, 0);
+            if (!good) {
               ok = false;
               break;
             }
-            if (lane == 0) {
-              const int j = (int)(((uint32_t)pw + (uint32_t)C::NPB - ci % (uint32_t)C::NPB) % (uint32_t)C::NPB);
-              if (k1 >= 0) {
-                const uint32_t slot = (tb + (uint32_t)j) % C::NB;
-                const uint32_t fb = smem_u32(&b_full[slot]);
-                mbar_arrive_expect_tx(fb, C::TILEB);
-                bulk_load_hint(smem0 + C::OFF_BR + slot * C::TILEB,
-                               p_bpack + ((int64_t)bcol * p_kbs + k1) * (4096 * C::NOPS), C::TILEB, fb, pol_b);
-              }
-              if (k2 >= 0) {
-                const uint32_t slot = (tb + (uint32_t)(j + C::NPB)) % C::NB;
-                const uint32_t fb = smem_u32(&b_full[slot]);
-                mbar_arrive_expect_tx(fb, C::TILEB);
-                bulk_load_hint(smem0 + C::OFF_BR + slot * C::TILEB,
-                               p_bpack + ((int64_t)bcol * p_kbs + k2) * (4096 * C::NOPS), C::TILEB, fb, pol_b);
-              }
-            }
-            tb += (uint32_t)n_t;
           }
         }
       }
     }
-    if (!ok) {
-      // every tile below tb was issued (a stage is issued whole or not at
-      // all): wait for the last one of each slot to land
-      named_bar_sync(1, 32 * C::NPB);
-      if (leader)
-        for (uint32_t x = 0; x < (uint32_t)C::NB && x < tb; ++x) {
-          const uint32_t last = x + (tb - 1 - x) / C::NB * C::NB;
-          mbar_wait_drain(smem_u32(&b_full[x]), (last / C::NB) & 1, err, lim);
-        }
+    if (!ok && lane == 0 && last_mine != 0xffffffffu) {
+      // wait for this warp's own copies still in flight: they can only be in
+      // the last NS stages it copied into
+      const uint32_t lo = last_mine + 1 > (uint32_t)C::NS ? last_mine + 1 - C::NS : 0;
+      for (uint32_t k = lo; k <= last_mine; ++k)
+        mbar_wait_drain(smem_u32(&full[k % C::NS]), (k / C::NS) & 1, err, lim);
     }
   } else if (warp < C::NMMA) {
     if (lane == 0) {
       // ----------------------------------------------------------- MMA issuers
       // Issuer w runs the MMA groups of its quarter of the panel's block rows,
-      // from the list the A copy brought in with the stage, and commits once
-      // per stage to the stage's done barrier (which frees the stage's A slot
-      // and B slots). It waits for the B tiles in order, every tile of every
-      // stage, the ones it does not read included, before that commit: a
-      // tile slot's barrier is then never waited on more than one phase
-      // ahead of the tile in it (a parity wait cannot tell phases two apart).
-      uint32_t ci = 0, k = 0, tb = 0, wup = 0;  // wup: tiles below it have landed
+      // from the list the copy brought in with the stage, and releases every
+      // stage once. One thread issues a tcgen05.mma only every ~80-150
+      // cycles; four keep the tensor pipe near its rate for these narrow MMAs.
+      uint32_t ci = 0, k = 0, slot_s = 0, phase_s = 0;
       bool ok = true, issued = false;
       const uint32_t stall = (blockIdx.x == 0 && warp == 0) ? (uint32_t)args.stall_stage : 0u;
       for (uint32_t kk = 0; ok; ++kk) {
@@ -564,54 +492,43 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
         const uint32_t idesc0 = P.idesc;  // without the N field
         const int nstages = wi.s1 - wi.s0;
         for (int nt = 0; nt < n_tiles && ok; ++nt, ++k) {
-          const uint32_t buf = k % C::NBUF;
+          const uint32_t buf = k & 1;
           const uint32_t dbase = tmem + buf * C::ACC_COLS;
-          // use u = k / NBUF of this buffer waits for phase u of accempty: the
+          // use u = k / 2 of this buffer waits for phase u of accempty: the
           // epilogue's initial zeroing (u = 0), then each drain-and-zero
-          if (!wait_phase(smem_u32(&accempty[buf]), (k / C::NBUF) & 1, abort_flag, err, ERR_MMA_ACC, lim)) {
+          if (!wait_phase(smem_u32(&accempty[buf]), (k >> 1) & 1, abort_flag, err, ERR_MMA_ACC, lim)) {
             ok = false;
             break;
           }
           tc_fence_after();
           for (int c = 0; c < nstages; ++c, ++ci) {
+            const uint32_t s = slot_s;  // == ci % NS, kept incrementally
             if (stall != 0u && ci + 1 == stall) {
               // test stall: nothing arrives on this barrier, so the wait runs
               // into its limit and the CTA aborts
               ok = wait_phase(smem_u32(stallbar), 0, abort_flag, err, ERR_MMA_STALL, lim);
               if (!ok) break;
             }
-            const uint32_t s = ci % C::NA;
-            // the stage's A copy landed (complete_tx); the MMA reads shared
+            // the stage's copies landed (complete_tx); the MMA reads shared
             // memory through the async proxy, so no tcgen05 fence is needed
-            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &a_full[s]), (ci / C::NA) & 1, abort_flag, err, ERR_MMA_A,
-                            lim)) {
+            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &full[s]), phase_s, abort_flag, err, ERR_MMA_A, lim)) {
               ok = false;
               break;
             }
-            const uint8_t* stp = smem + s * C::ASLOT;
-            const uint32_t hw = (uint32_t)a_hw[s];
+            const uint8_t* stp = smem + s * C::STAGE;
+            const uint32_t hw = *reinterpret_cast<const uint32_t*>(stp + C::OFF_HW);
             const uint32_t wl = *reinterpret_cast<const uint16_t*>(stp + hw + 2 * warp);
-            const uint32_t ntl = *reinterpret_cast<const uint16_t*>(stp + hw + 10);
             const uint32_t first = wl & 0xffu, cnt = wl >> 8;
             const uint32_t* ent = reinterpret_cast<const uint32_t*>(stp + hw + kStageHdrFixed) + first;
-            // descriptors of operands = the smem base's descriptor + offset / 16
-            const uint64_t sdesc = desc_kmajor_sw32(smem0);
-            const uint32_t a_off = s * C::ASLOT;
-            for (uint32_t e = 0; e < cnt && ok; ++e) {
+            // descriptors of operands inside the stage = stage descriptor + offset / 16
+            const uint64_t sdesc = desc_kmajor_sw32(smem0 + s * C::STAGE);
+            for (uint32_t e = 0; e < cnt; ++e) {
               const uint32_t m = ent[e];
               const uint32_t pos = m & 31u, tile = (m >> 5) & 15u, slot = (m >> 9) & 31u;
               const uint32_t len = ((m >> 14) & 15u) + 1u, acc = (m >> 18) & 1u;
-              const uint32_t tpos = tb + tile;
-              const uint32_t bslot = tpos % C::NB;
-              for (; wup <= tpos; ++wup)
-                if (!wait_phase(smem_u32(&b_full[wup % C::NB]), (wup / C::NB) & 1, abort_flag, err, ERR_MMA_B, lim)) {
-                  ok = false;
-                  break;
-                }
-              if (!ok) break;
               const uint32_t idesc = idesc0 | (((len * BH) >> 3) << 17);
-              const uint64_t a_hi = sdesc + ((a_off + pos * C::ABLK) >> 4);
-              const uint64_t b_hi0 = sdesc + ((C::OFF_BR + bslot * C::TILEB) >> 4);
+              const uint64_t a_hi = sdesc + ((pos * C::ABLK) >> 4);
+              const uint64_t b_hi0 = sdesc + ((C::OFF_B + tile * C::TILEB) >> 4);
 #pragma unroll
               for (int j = 0; j < NSUB; ++j) {
                 const uint32_t dcol = dbase + j * C::SUB_COLS + slot * BH;
@@ -626,12 +543,11 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               }
               issued = true;
             }
-            for (; ok && wup < tb + ntl; ++wup)
-              if (!wait_phase(smem_u32(&b_full[wup % C::NB]), (wup / C::NB) & 1, abort_flag, err, ERR_MMA_B, lim))
-                ok = false;
-            if (!ok) break;
-            umma_commit(smem_u32(&done[ci % C::NSD]));
-            tb += ntl;
+            umma_commit(smem_u32(&empty[s]));
+            if (++slot_s == (uint32_t)C::NS) {
+              slot_s = 0;
+              phase_s ^= 1u;
+            }
           }
           if (!ok) break;
           umma_commit(smem_u32(&accfull[buf]));
@@ -651,12 +567,14 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     // a part that starts in the middle of a panel accumulates onto zero.
     const uint32_t q = warp & 3;
     const uint32_t lane_base = tmem + ((q * 32u) << 16);
-    for (uint32_t c = 0; c < C::TMEM_COLS; c += 16) tmem_st_x16_zero(lane_base + c);
+    for (uint32_t c = 0; c < 2 * C::ACC_COLS; c += 16) tmem_st_x16_zero(lane_base + c);
     tmem_st_wait();
     tc_fence_before();
     __syncwarp();
-    if (lane == 0)
-      for (int b = 0; b < C::NBUF; ++b) mbar_arrive(smem_u32(&accempty[b]));
+    if (lane == 0) {
+      mbar_arrive(smem_u32(&accempty[0]));
+      mbar_arrive(smem_u32(&accempty[1]));
+    }
     constexpr int SLAB = R * BH * C::BN;  // floats per slab
     constexpr int PW = (R % kMmaWarps == 0) ? R / kMmaWarps : 0;  // slots per issuing warp
     constexpr int RPL = (R * BH + 31) / 32;                          // C-row entries per lane
@@ -704,8 +622,8 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
                        : -1;
       }
       for (int nt = 0; nt < n_tiles; ++nt, ++k) {
-        const uint32_t buf = k % C::NBUF;
-        if (!warp_wait(smem_u32(&accfull[buf]), (k / C::NBUF) & 1, lane, abort_flag, err, ERR_EPI, true, lim)) {
+        const uint32_t buf = k & 1;
+        if (!warp_wait(smem_u32(&accfull[buf]), (k >> 1) & 1, lane, abort_flag, err, ERR_EPI, true, lim)) {
           ok = false;
           break;
         }
@@ -908,21 +826,16 @@ static int ctas_per_sm_one() {
   X(16, 4, 1, 0)            \
   X(16, 8, 1, 0)            \
   X(16, 16, 1, 0)           \
-  X(16, 32, 1, 0)           \
   X(32, 4, 1, 0)            \
   X(32, 8, 1, 0)            \
-  X(32, 16, 1, 0)           \
   X(16, 4, 1, 1)            \
   X(16, 8, 1, 1)            \
   X(16, 16, 1, 1)           \
-  X(16, 32, 1, 1)           \
   X(32, 4, 1, 1)            \
   X(32, 8, 1, 1)            \
-  X(32, 16, 1, 1)           \
   X(16, 4, 1, 2)            \
   X(16, 8, 1, 2)            \
-  X(16, 16, 1, 2)           \
-  X(16, 32, 1, 2)
+  X(16, 16, 1, 2)
 
 bool tc_variant_supported(int bh, int R, int nsub, int kind) {
 #define SMAT_TC_MATCH(BH, R_, NS, K) \

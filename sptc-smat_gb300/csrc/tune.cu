@@ -91,7 +91,7 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
     out->cached = 1;
     return SMAT_OK;
   }
-  const std::vector<int> Rs = bh == 16 ? std::vector<int>{4, 8, 16, 32} : std::vector<int>{4, 8, 16};
+  const std::vector<int> Rs = bh == 16 ? std::vector<int>{4, 8, 16} : std::vector<int>{4, 8};
   const std::vector<float> fracs = {-1.0f, 2.0f, 1.0f, 0.5f};
   int prev = -1;
   cudaGetDevice(&prev);
