@@ -357,9 +357,9 @@ def run_smat(args):
 
     # the same step with the structured-sparse path on: exact-2:4 blocks on
     # tcgen05.mma.sp (second launch), the others on the dense kernel
-    sp24 = None
-    if not args.no_sp24:
-        M24 = smat.Bcsr(A, block=(16, 16), forms=(smat.FORM_F16,), row_perm=perm, device=local, use_24=True)
+    sp24 = []
+    for unit_min in ([] if args.no_sp24 else [1, 8]):
+        M24 = smat.Bcsr(A, block=(16, 16), forms=(smat.FORM_F16,), row_perm=perm, device=local, use_24=unit_min)
         ws24_bytes = M24.workspace_size(smat.FORM_F16, smat.F16, N)
         ws24 = torch.empty(ws24_bytes, dtype=torch.uint8, device=dev)
         C24 = torch.empty((A.rows, N), dtype=torch.float32, device=dev)
@@ -394,12 +394,14 @@ def run_smat(args):
         i24 = M24.info
         # 2:4 blocks move 256 B of kept values + 32 B of metadata instead of 512 B
         n24 = i24["n_blocks_24"]
-        sp24 = {"value": world * 2.0 * A.nnz * N / (ms24 * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms24,
+        sp24.append({"unit_min_blocks": unit_min,
+                "value": world * 2.0 * A.nnz * N / (ms24 * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms24,
                 "n_blocks_24": n24, "nnzb": i24["nnzb"], "rel_err_vs_fp64": err24,
                 "a_bytes": (i24["nnzb"] - n24) * 512 + n24 * 288, "a_bytes_dense_path": i24["nnzb"] * 512,
                 "step": "pack B (4 KB tiles, then 8 KB 2:4 windows) + dense SpMM over the other blocks + "
-                        "tcgen05.mma.sp over the exact-2:4 blocks (4 launches), one CUDA graph"}
-        log(f"[bench] 2:4 path: {n24} of {i24['nnzb']} blocks on mma.sp, {ms24:.4f} ms/step, rel err {err24:.3e}")
+                        "tcgen05.mma.sp over the routed exact-2:4 blocks (4 launches), one CUDA graph"})
+        log(f"[bench] 2:4 path (units of >= {unit_min}): {n24} of {i24['nnzb']} blocks on mma.sp, "
+            f"{ms24:.4f} ms/step, rel err {err24:.3e}")
         M24.close()
         del ws24, C24
 
@@ -460,7 +462,7 @@ def run_smat(args):
                 "h2d_bytes_per_step": A.cols * N * 2, "d2h_bytes_per_step": A.rows * N * 4, "ms_per_step": e2e_ms},
         "gpu_launches": 2 * args.steps,
     }
-    if sp24 is not None:
+    if sp24:
         line["sp24_path"] = sp24
     if rank == 0:
         cpu_v, sample = cpu_baseline(A, N, threads=1, budget_s=12.0)
@@ -588,6 +590,64 @@ def run_libraries(args):
         del S, B, out
 
 
+PRUNED24_WORKLOAD = {
+    "workload": "pruned24_randomblock65536_N128",
+    "generator": "65536 x 65536, random 16x16 blocks at 2 % block density (60-90 % fill), then every block "
+                 "rewritten to an exact 2:4 pattern (2 nonzeros in every aligned group of 4 columns of every "
+                 "row, values N(0,1)): a 2:4-pruned block-sparse matrix; B 65536x128 FP16 U[-1,1]; FP32 C",
+    "N": 128,
+}
+
+
+def run_pruned24(args):
+    """The structured-sparse path where every block is exactly 2:4: one JSON
+    line for the dense path and one per 2:4 routing threshold (use_24 = the
+    fewest exact-2:4 blocks a unit of 8 block rows x 32 columns must hold)."""
+    import torch
+
+    import smat
+    from smat import generators as G
+    dev = torch.device("cuda", 0)
+    A = G.force_24(G.random_block(65536, 0.02, 0.6, 0.9, seed=3), 1.0, seed=4)
+    N = PRUNED24_WORKLOAD["N"]
+    Bh = np.random.default_rng(1).uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    import scipy.sparse as sps
+    ref = sps.csr_matrix((A.values.astype(np.float64), A.col_idx, A.row_ptr), shape=(A.rows, A.cols)) @ \
+        Bh.astype(np.float64)
+    B = torch.from_numpy(Bh).to(dev)
+    useful = 2.0 * A.nnz * N
+    for unit_min in (0, 1, 8):
+        M = smat.Bcsr(A, use_24=unit_min)
+        C = M.spmm(B)
+        torch.cuda.synchronize(dev)
+        M.check_device_error()
+        err = float(np.linalg.norm(C.double().cpu().numpy() - ref) / np.linalg.norm(ref))
+        ws = torch.empty(M.workspace_size(smat.FORM_F16, smat.F16, N), dtype=torch.uint8, device=dev)
+        for _ in range(max(args.warmup, 3)):
+            M.spmm(B, out=C, workspace=ws)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            M.spmm(B, out=C, workspace=ws)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        M.check_device_error()
+        ms = e0.elapsed_time(e1) / args.steps
+        inf = M.info
+        n24 = inf["n_blocks_24"]
+        print(json.dumps({"metric": METRIC, "value": useful / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                          "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                          "data": "synthetic", "dtype": "f16", "rel_err_vs_fp64": err,
+                          "config": {k: PRUNED24_WORKLOAD[k] for k in ("workload", "generator", "N")} |
+                          {"nnz": A.nnz, "nnzb": inf["nnzb"], "use_24": unit_min, "n_blocks_24": n24,
+                           "a_bytes": (inf["nnzb"] - n24) * 512 + n24 * 288,
+                           "step": "pack B + dense SpMM" + (" + 2:4 B windows + tcgen05.mma.sp SpMM" if n24 else "")
+                           + ", eager calls"}}), flush=True)
+        M.close()
+        del C, ws
+
+
 BATCH_WORKLOAD = {
     "workload": "batched512_uneven",
     "generator": "512 matrices, rows log-uniform in [1024, 32768]; 1/3 band (half-bandwidth 8-256), 1/3 R-MAT "
@@ -668,7 +728,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="smat", choices=["smat", "reference"])
     ap.add_argument("--workload", default="rmat16",
-                    choices=["rmat16", "stencil64_forms", "batched512", "rmat16_libraries", "rmat16_reorder"],
+                    choices=["rmat16", "stencil64_forms", "batched512", "rmat16_libraries", "rmat16_reorder",
+                             "pruned24"],
                     help="rmat16: the headline SpMM line; stencil64_forms: one line per precision form; "
                          "batched512: grouped vs sequential SpMMs; rmat16_libraries: cuSPARSE on the "
                          "headline inputs, for comparison; rmat16_reorder: the reorder step alone "
@@ -686,6 +747,8 @@ def main():
         run_batched(args)
     elif args.workload == "rmat16_libraries":
         run_libraries(args)
+    elif args.workload == "pruned24":
+        run_pruned24(args)
     else:
         run_smat(args)
 

@@ -71,7 +71,13 @@ typedef struct smat_bcsr_opts {
   int32_t block_rows;     /* bh: 16 (default when 0) */
   int32_t block_cols;     /* bw: 16 (default when 0) */
   uint32_t forms;         /* bit (1 << smat_form) per form to materialise; 0 = F16 only */
-  int32_t use_24;         /* 1: blocks that are exactly 2:4 use the sparse tensor-core path */
+  int32_t use_24;         /* 0: off. k > 0: a block that is exactly 2:4 (at most two nonzeros
+                             in every aligned group of four columns of every row) runs on the
+                             structured-sparse tensor-core path (FP16 / BF16 forms, 16 x 16
+                             blocks) when its unit -- 8 block rows x one 32-column window --
+                             holds at least k such blocks; 1 = every such block, as the
+                             reference routes them (mmaOBTS_large.cu:19-254); the other
+                             blocks stay on the dense path */
   const int64_t* row_perm;/* (host, optional) new row r = old row row_perm[r]; SpMM results
                              are written back in the ORIGINAL row order */
   int32_t device;         /* CUDA device ordinal */
@@ -95,7 +101,7 @@ typedef struct smat_bcsr_info {
   int64_t rows_padded, cols_padded;
   int64_t nnz;                  /* scalar nonzeros stored in the input CSR */
   int64_t nnzb;                 /* nonzero blocks */
-  int64_t n_blocks_24;          /* blocks that are exactly 2:4 (0 unless use_24) */
+  int64_t n_blocks_24;          /* blocks routed to the 2:4 path (0 unless use_24) */
   int32_t block_rows, block_cols;
   int32_t panel_rows;
   int32_t n_panels;

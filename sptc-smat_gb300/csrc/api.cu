@@ -133,21 +133,24 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   // the split form, class 2 the FP8 form
   // the structured-sparse path takes the exact-2:4 blocks of the FP16 and
   // BF16 forms (16 x 16 blocks); their plan (class 0) leaves them out
-  h->sp24_on = h->use24 && bh == 16 && bw == 16 &&
-               (forms & ((1u << SMAT_FORM_F16) | (1u << SMAT_FORM_BF16))) &&
-               std::any_of(h->host.is24.begin(), h->host.is24.end(), [](uint8_t v) { return v != 0; });
+  // (use_24 = the fewest such blocks a unit -- 8 block rows x 32 columns --
+  // must hold for its blocks to be routed there)
+  std::vector<uint8_t> take24;
+  if (h->use24 > 0 && bh == 16 && bw == 16 && (forms & ((1u << SMAT_FORM_F16) | (1u << SMAT_FORM_BF16))))
+    route_sp24(h->host, h->use24, take24);
+  h->sp24_on = std::any_of(take24.begin(), take24.end(), [](uint8_t v) { return v != 0; });
   for (int cls = 0; cls < kPlanClasses; cls++) {
     if (cls == 1 && !(forms & (1u << SMAT_FORM_SPLIT_BF16))) continue;
     if (cls == 2 && !(forms & (1u << SMAT_FORM_FP8))) continue;
-    st = build_plan(h->host, R, cls, h->pc[cls].plan, (cls == 0 && h->sp24_on) ? &h->host.is24 : nullptr);
+    st = build_plan(h->host, R, cls, h->pc[cls].plan, (cls == 0 && h->sp24_on) ? &take24 : nullptr);
     if (st != SMAT_OK) {
       delete h;
       return st;
     }
     h->pc[cls].built = true;
   }
-  for (uint8_t v : h->host.is24) h->n_24 += v;
-  if (!h->sp24_on) h->n_24 = 0;
+  if (h->sp24_on)
+    for (uint8_t v : take24) h->n_24 += v;
 
 #define SMAT_TRY(x)              \
   do {                           \
@@ -164,10 +167,10 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     Sp24Host sp;
     for (int fmt = 0; fmt < 2; fmt++) {
       if (!(forms & (1u << (fmt == 0 ? SMAT_FORM_F16 : SMAT_FORM_BF16)))) continue;
-      SMAT_TRY(build_sp24(b, b.is24, fmt, sp));
+      SMAT_TRY(build_sp24(b, take24, fmt, sp));
       SMAT_TRY(upload(&h->d_sp24_stream[fmt], sp.stream.data(), sp.stream.size()));
     }
-    // (some block is exactly 2:4, so every list below has an entry)
+    // (some block is routed to the 2:4 path, so every list below has an entry)
     SMAT_TRY(upload(&h->d_sp24_stages, sp.stages.data(), sp.stages.size()));
     SMAT_TRY(upload(&h->d_sp24_groups, sp.groups.data(), sp.groups.size()));
     SMAT_TRY(upload(&h->d_sp24_unit_window, sp.unit_window.data(), sp.unit_window.size()));

@@ -106,6 +106,9 @@ struct Sp24Host {
   int64_t n_blocks = 0, n_units = 0;
 };
 smat_status build_sp24(const HostBcsr& b, const std::vector<uint8_t>& take, int fmt, Sp24Host& out);
+// Blocks routed to the 2:4 path: exactly 2:4 (is24), in a unit (8 block
+// rows x one 32-column window) holding at least min_unit such blocks.
+void route_sp24(const HostBcsr& b, int min_unit, std::vector<uint8_t>& take);
 
 // The reference's per-block sparsity label (csrToBcsr, matrix.h:679-711), per
 // BCSR block: 1 = "2:4" (the default), 2 = dense once a row of the block has

@@ -34,6 +34,31 @@ inline uint32_t compress_group(const uint16_t* f16, const uint16_t* out_vals, ui
 
 }  // namespace
 
+void route_sp24(const HostBcsr& b, int min_unit, std::vector<uint8_t>& take) {
+  const int64_t nbr = b.nbr(), nnzb = b.nnzb();
+  take.assign(nnzb, 0);
+  if (b.bh != 16 || b.bw != 16 || min_unit < 1) return;
+  // count the exact-2:4 blocks of every unit of a group, window by window
+  std::vector<int32_t> cnt;
+  for (int64_t g0 = 0; g0 < nbr; g0 += kSp24GroupRows) {
+    const int64_t g1 = std::min<int64_t>(nbr, g0 + kSp24GroupRows);
+    for (int pass = 0; pass < 3; pass++)
+      for (int64_t br = g0; br < g1; br++)
+        for (int32_t k = b.rowptr[br]; k < b.rowptr[br + 1]; k++) {
+          if (!b.is24[k]) continue;
+          const int32_t w = b.colidx[k] / 32;
+          if (pass == 0) {
+            if ((size_t)w >= cnt.size()) cnt.resize((size_t)w + 1, 0);
+            cnt[w]++;
+          } else if (pass == 1) {
+            take[k] = cnt[w] >= min_unit ? 1 : 0;
+          } else {
+            cnt[w] = 0;  // reset for the next group
+          }
+        }
+  }
+}
+
 smat_status build_sp24(const HostBcsr& b, const std::vector<uint8_t>& take, int fmt, Sp24Host& out) {
   out = Sp24Host{};
   if (b.bh != 16 || b.bw != 16) return fail(SMAT_ERR_UNSUPPORTED, "2:4 path: 16 x 16 blocks only");

@@ -55,7 +55,7 @@ struct Sp24Cfg {
   static constexpr uint32_t STAGE_SLOT = (STAGE_MAX + 1023) / 1024 * 1024;
   static constexpr int NT = 4;                                   // A tile slots (and metadata columns)
   static constexpr uint32_t ATILE = 128 * 32;                    // 128 rows x 16 kept values
-  static constexpr int NBT = 6;                                  // B tile slots
+  static constexpr int NBT = 12;                                 // B tile slots (8 KB copies from L2 in flight)
   static constexpr uint32_t BTILE = 128 * 64;                    // 128 columns x 32 k
   static constexpr uint32_t OFF_A = NS * STAGE_SLOT;
   static constexpr uint32_t OFF_B = OFF_A + NT * ATILE;

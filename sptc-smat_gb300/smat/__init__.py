@@ -240,7 +240,7 @@ class Bcsr:
         o.forms = 0
         for f in forms:
             o.forms |= 1 << f
-        o.use_24 = 1 if use_24 else 0
+        o.use_24 = int(use_24)          # True: every exact-2:4 block; k > 1: units of >= k such blocks
         self._perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
         o.row_perm = None if self._perm is None else self._perm.ctypes.data
         o.device = device

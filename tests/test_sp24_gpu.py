@@ -95,3 +95,23 @@ def test_same_as_dense_path(dev, smat_mod):
     assert np.array_equal(c1, c1b)
     M0.close()
     M1.close()
+
+
+def test_unit_threshold_routing(dev, smat_mod, oracle_lib):
+    """use_24 = k routes only the exact-2:4 blocks of units (8 block rows x
+    32 columns) holding at least k of them; the rest stay dense."""
+    A = matrix("mixed", smat_mod)
+    Bh = np.random.default_rng(5).uniform(-1, 1, (A.cols, 128)).astype(np.float16)
+    ref = fp64_product(oracle_lib, A, Bh)
+    B = torch.from_numpy(Bh).to(dev)
+    counts = []
+    for k in (1, 2, 4, 8, 17):
+        M = smat_mod.Bcsr(A, use_24=k)
+        counts.append(M.info["n_blocks_24"])
+        err = rel_err(run(M, B, smat_mod.FORM_F16), ref)
+        assert err <= 1e-3, (k, err)
+        M.close()
+    print("2:4 blocks routed for unit thresholds 1, 2, 4, 8, 17:", counts)
+    assert counts[0] > counts[1] > counts[2] > 0
+    assert all(a >= b for a, b in zip(counts, counts[1:]))
+    assert counts[-1] == 0                        # a unit holds at most 16 blocks
