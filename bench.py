@@ -486,8 +486,11 @@ FORMS_WORKLOAD = {
 
 
 def run_forms(args):
-    """The precision forms on the stencil workload: one JSON line per form with
-    its useful TFLOP/s (pack B + contraction) and its error against FP64."""
+    """The precision forms on the stencil workload: per form one JSON line
+    with the default tile shape and one with the shape smat_autotune measured
+    fastest for it (panel rows x split threshold x N-tile width x pipeline
+    depth), each with its useful TFLOP/s (pack B + contraction) and its error
+    against FP64."""
     import torch
 
     import smat
@@ -508,17 +511,18 @@ def run_forms(args):
     nrm = np.linalg.norm(ref)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
-    info = M.info
-    for name, f in forms.items():
-        ws_bytes = M.workspace_size(f, smat.F32, N)
+    useful = 2.0 * A.nnz * N
+
+    def measure(Mh, f):
+        ws_bytes = Mh.workspace_size(f, smat.F32, N)
         ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
 
         def step():
-            M.spmm_raw(f, B, smat.F32, smat.ROW_MAJOR, N, Cd, smat.F32, N, N, ws, ws_bytes, sp)
+            Mh.spmm_raw(f, B, smat.F32, smat.ROW_MAJOR, N, Cd, smat.F32, N, N, ws, ws_bytes, sp)
 
         step()
         torch.cuda.synchronize(dev)
-        M.check_device_error()
+        Mh.check_device_error()
         err = float(np.linalg.norm(Cd.cpu().numpy().astype(np.float64) - ref) / nrm)
         for _ in range(max(args.warmup, 3)):
             step()
@@ -529,14 +533,32 @@ def run_forms(args):
             step()
         e1.record(stream)
         torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / args.steps
-        useful = 2.0 * A.nnz * N
-        print(json.dumps({"metric": METRIC, "form": name, "value": useful / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-                          "ms_per_step": ms, "rel_err_vs_fp64": err, "steps": args.steps, "warmup": args.warmup,
-                          "higher_is_better": True, "data": "synthetic",
+        Mh.check_device_error()
+        return e0.elapsed_time(e1) / args.steps, err
+
+    def emit(name, shape, ms, err, info):
+        print(json.dumps({"metric": METRIC, "form": name, "shape": shape, "value": useful / (ms * 1e-3) / 1e12,
+                          "unit": "TFLOP/s", "ms_per_step": ms, "rel_err_vs_fp64": err, "steps": args.steps,
+                          "warmup": args.warmup, "higher_is_better": True, "data": "synthetic",
                           "config": dict(FORMS_WORKLOAD, nnz=A.nnz, nnzb=info["nnzb"], fill=info["fill"],
-                                         panel_rows=info["panel_rows"])}), flush=True)
-        del ws
+                                         panel_rows=info["panel_rows"], n_tile_cols=info["n_tile_cols"],
+                                         pipeline_depth=info["pipeline_depth"])}), flush=True)
+
+    for name, f in forms.items():
+        ms, err = measure(M, f)
+        emit(name, "default", ms, err, M.info)
+    M.close()
+    if args.no_tune:
+        return
+    for name, f in forms.items():
+        t0 = time.time()
+        r = smat.autotune(A, form=f, N=N)
+        log(f"[bench] {name}: autotune {r} in {time.time() - t0:.0f}s")
+        Mt = smat.Bcsr(A, forms=(f,), panel_rows=r["panel_rows"], split_frac=r["split_frac"],
+                       n_tile_cols=r["n_tile_cols"], pipeline_depth=r["pipeline_depth"])
+        ms, err = measure(Mt, f)
+        emit(name, "autotuned", ms, err, Mt.info)
+        Mt.close()
 
 
 def run_libraries(args):
@@ -736,6 +758,7 @@ def main():
                          "(with --impl reference: the reference's own reorder)")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--no-sp24", action="store_true", help="skip the structured-sparse (2:4) path's line")
+    ap.add_argument("--no-tune", action="store_true", help="stencil forms: skip the autotuned lines")
     args = ap.parse_args()
     if args.workload == "rmat16_reorder":
         run_reorder(args)

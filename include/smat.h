@@ -92,6 +92,14 @@ typedef struct smat_bcsr_opts {
                              reordering, src/reorder.py:140-182) and smat_spmm gathers B's
                              rows through the same permutation, so C = A * B unchanged;
                              smat_bcsr_export then shows the permuted columns */
+  int32_t n_tile_cols;    /* 0 or 128: C is computed 128 columns per pass over A; 256: with
+                             panel_rows <= 8 the handle also holds a plan for 256-column
+                             passes, which the FP16 and BF16 forms use for N > 128 (A read
+                             once per 256 columns; one more copy of A on the device);
+                             with panel_rows = 0 the autotuner's cached choice */
+  int32_t pipeline_depth; /* pipeline stages in flight (2..): 0 = as many as fit in shared
+                             memory (3 for the default stage shapes), or the autotuner's
+                             cached choice when panel_rows = 0 */
 } smat_bcsr_opts;
 
 typedef struct smat_bcsr smat_bcsr; /* opaque handle, immutable after create */
@@ -107,6 +115,8 @@ typedef struct smat_bcsr_info {
   int32_t n_panels;
   int64_t n_union_cols;         /* B tiles one SpMM pass loads (per N tile) */
   double fill;                  /* nnz / (nnzb * bh * bw) */
+  int32_t n_tile_cols;          /* widest N tile the handle runs: 128, or 256 (FP16 / BF16, N > 128) */
+  int32_t pipeline_depth;       /* stages in flight requested (0: all that fit) */
 } smat_bcsr_info;
 
 typedef struct smat_reorder_stats {
@@ -279,21 +289,26 @@ smat_status smat_spmm_static_scratch(const smat_bcsr* A, int32_t form, const voi
 /* ---------------------------------------------------------------- autotuner */
 
 typedef struct smat_tune_result {
-  int32_t panel_rows;   /* block rows per panel that measured fastest */
+  int32_t panel_rows;   /* block rows per panel (block rows per CTA work item) that measured fastest */
   float split_frac;     /* panel splitting threshold that measured fastest (< 0: none) */
   double ms;            /* its SpMM time (pack B + contraction), milliseconds */
   double ms_default;    /* the default shape's time, for comparison (0 if cached) */
   int32_t cached;       /* 1: answered from the cache without measuring */
+  int32_t n_tile_cols;  /* N-tile width that measured fastest: 128 or 256 */
+  int32_t pipeline_depth; /* stages in flight that measured fastest (0: all that fit) */
+  int32_t candidates;   /* shapes measured (0 if cached) */
 } smat_tune_result;
 
-/* Measures the launch shapes offered for A (block rows per panel, and the
- * panel-splitting threshold) for this form and N on opts->device, and keeps
- * the fastest in a process-wide cache keyed on A's block-density statistics
- * (blocks per block row, blocks per B tile in a 16-row panel), the N-tile
- * count and the form's kernel. Later smat_bcsr_create calls with
- * panel_rows = 0 use the cached shape for matrices with the same key. No
- * counterpart in the reference (its tile shape is fixed at compile time).
- * Allocates device memory for its trial runs and synchronises. */
+/* Measures the launch shapes offered for A on opts->device for this form and
+ * N -- block rows per panel x panel-splitting threshold x N-tile width (128,
+ * or 256 when N > 128 and the panel has at most 8 block rows), then the
+ * pipeline depth of the best of those -- and keeps the fastest in a
+ * process-wide cache keyed on A's block-density statistics (blocks per
+ * block row, blocks per B tile in a 16-row panel), the N-tile count and the
+ * form's kernel. Later smat_bcsr_create calls with panel_rows = 0 use the
+ * cached shape for matrices with the same statistics. No counterpart in the
+ * reference (its tile shape is fixed at compile time). Allocates device
+ * memory for its trial runs and synchronises. */
 smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t form, int64_t N,
                           smat_tune_result* out);
 smat_status smat_autotune_clear(void);

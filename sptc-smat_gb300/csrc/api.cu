@@ -79,7 +79,8 @@ static void free_handle(smat_bcsr* h) {
   cudaSetDevice(h->device);
   void* ptrs[] = {h->d_kperm, h->d_aval[0], h->d_aval[1], h->d_aval[2], h->d_aval[3], h->d_err,
                   h->d_bstage, h->d_cstage, h->d_ws, h->d_sp24_stages, h->d_sp24_groups,
-                  h->d_sp24_unit_window, h->d_sp24_stream[0], h->d_sp24_stream[1], h->d_bcsr_row_map};
+                  h->d_sp24_unit_window, h->d_sp24_stream[0], h->d_sp24_stream[1], h->d_bcsr_row_map,
+                  h->d_aval_wide[0], h->d_aval_wide[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (PlanDev& pd : h->pc) {
@@ -98,7 +99,9 @@ int smat::kind_of(int32_t form) {
 }
 
 int smat::pick_nsub(const smat_bcsr* h, int64_t N, int kind) {
-  if (N > 128 && kind == TC_KIND_PLAIN && tc_variant_supported(h->host.bh, h->R, 2, kind)) return 2;
+  // 256-column passes where the handle holds their plan (opts.n_tile_cols)
+  if (N > 128 && kind == TC_KIND_PLAIN && h->pc[3].built && tc_variant_supported(h->host.bh, h->R, 2, kind))
+    return 2;
   return 1;
 }
 
@@ -113,17 +116,27 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   // heavy panels are split over CTAs below
   int R = o.panel_rows ? o.panel_rows : default_panel_rows(bh);
   float split_frac = o.split_frac;
+  int ntc = o.n_tile_cols, depth = o.pipeline_depth;
   if (o.panel_rows == 0) {
     // a configuration the autotuner measured for matrices like this one
-    TuneKey key;
-    if (tune_key_of(h->host, kind_of(SMAT_FORM_F16), 128, key)) {
+    // (measured for N <= 128 first, else for N <= 256)
+    for (int64_t n_try : {128, 256}) {
+      TuneKey key;
       TuneVal tv;
-      if (tune_lookup(key, tv)) {
+      if (tune_key_of(h->host, kind_of(SMAT_FORM_F16), n_try, key) && tune_lookup(key, tv)) {
         R = tv.panel_rows;
         if (o.split_frac == 0.0f) split_frac = tv.split_frac;
+        if (o.n_tile_cols == 0) ntc = tv.n_tile_cols;
+        if (o.pipeline_depth == 0) depth = tv.depth;
+        break;
       }
     }
   }
+  if ((ntc != 0 && ntc != 128 && ntc != 256) || depth < 0 || depth == 1) {
+    delete h;
+    return fail(SMAT_ERR_INVALID, "n_tile_cols must be 0, 128 or 256 and pipeline_depth 0 or >= 2");
+  }
+  h->depth = depth;
   if (!tc_variant_supported(bh, R, 1, TC_KIND_PLAIN)) {
     delete h;
     return fail(SMAT_ERR_UNSUPPORTED, "unsupported panel_rows for this block height");
@@ -139,10 +152,13 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   if (h->use24 > 0 && bh == 16 && bw == 16 && (forms & ((1u << SMAT_FORM_F16) | (1u << SMAT_FORM_BF16))))
     route_sp24(h->host, h->use24, take24);
   h->sp24_on = std::any_of(take24.begin(), take24.end(), [](uint8_t v) { return v != 0; });
+  const bool wide = ntc == 256 && (forms & ((1u << SMAT_FORM_F16) | (1u << SMAT_FORM_BF16))) &&
+                    tc_variant_supported(bh, R, 2, TC_KIND_PLAIN);
   for (int cls = 0; cls < kPlanClasses; cls++) {
     if (cls == 1 && !(forms & (1u << SMAT_FORM_SPLIT_BF16))) continue;
     if (cls == 2 && !(forms & (1u << SMAT_FORM_FP8))) continue;
-    st = build_plan(h->host, R, cls, h->pc[cls].plan, (cls == 0 && h->sp24_on) ? &take24 : nullptr);
+    if (cls == 3 && !wide) continue;
+    st = build_plan(h->host, R, cls, h->pc[cls].plan, ((cls == 0 || cls == 3) && h->sp24_on) ? &take24 : nullptr);
     if (st != SMAT_OK) {
       delete h;
       return st;
@@ -193,7 +209,7 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     // parts so that no CTA gets much more than the average
     const int kind = cls == 1 ? TC_KIND_SPLIT : (cls == 2 ? TC_KIND_FP8 : TC_KIND_PLAIN);
     for (int nsub = 1; nsub <= 2; nsub++) {
-      if (!tc_variant_supported(bh, R, nsub, kind)) continue;
+      if (plan_class_of_kind(kind, nsub) != cls || !tc_variant_supported(bh, R, nsub, kind)) continue;
       const int per_sm = tc_ctas_per_sm(bh, R, nsub, kind);
       const int workers = std::max(1, h->num_sms * per_sm);
       std::vector<WorkItem> items;
@@ -241,6 +257,10 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
   if (forms & (1u << SMAT_FORM_F16)) {
     stream_layout(h->pc[0].plan, b.val_f16, nullptr, lay);
     SMAT_TRY(upload(&h->d_aval[SMAT_FORM_F16], lay.data(), lay.size()));
+    if (wide) {
+      stream_layout(h->pc[3].plan, b.val_f16, nullptr, lay);
+      SMAT_TRY(upload(&h->d_aval_wide[0], lay.data(), lay.size()));
+    }
   }
   if (forms & ((1u << SMAT_FORM_BF16) | (1u << SMAT_FORM_SPLIT_BF16))) {
     std::vector<uint16_t> hi(nval), lo(nval);
@@ -251,6 +271,10 @@ static smat_status finish_handle(smat_bcsr* h, const smat_bcsr_opts& o, smat_bcs
     if (forms & (1u << SMAT_FORM_BF16)) {
       stream_layout(h->pc[0].plan, hi, nullptr, lay);
       SMAT_TRY(upload(&h->d_aval[SMAT_FORM_BF16], lay.data(), lay.size()));
+      if (wide) {
+        stream_layout(h->pc[3].plan, hi, nullptr, lay);
+        SMAT_TRY(upload(&h->d_aval_wide[1], lay.data(), lay.size()));
+      }
     }
     if (forms & (1u << SMAT_FORM_SPLIT_BF16)) {
       stream_layout(h->pc[1].plan, hi, &lo, lay);
@@ -457,6 +481,8 @@ smat_status smat_bcsr_get_info(const smat_bcsr* A, smat_bcsr_info* info) {
     info->n_union_cols = u;
   }
   info->fill = b.nnzb() ? (double)b.nnz / ((double)b.nnzb() * b.bh * b.bw) : 0.0;
+  info->n_tile_cols = A->pc[3].built ? 256 : 128;
+  info->pipeline_depth = A->depth;
   return SMAT_OK;
 }
 
@@ -503,7 +529,7 @@ WsLayout smat::ws_layout(const smat_bcsr* A, int32_t form, int64_t N) {
     w.counters += (packed_b64_bytes(A->host.cols, std::max<int64_t>(N, 1)) + 255) / 256 * 256;
   }
   const int nsub = pick_nsub(A, N, kind_of(form));
-  const Sched& sc = A->pc[plan_class(form)].sched[nsub];
+  const Sched& sc = A->pc[plan_class(form, nsub)].sched[nsub];
   const int64_t bn = 128 * nsub, n_tiles = (std::max<int64_t>(N, 1) + bn - 1) / bn;
   w.counter_bytes = (16 + (size_t)sc.n_split * n_tiles * 4 * sizeof(int32_t) + 255) / 256 * 256;
   w.slabs = w.counters + w.counter_bytes;
@@ -520,17 +546,18 @@ void smat::fill_problem(const smat_bcsr* A, int32_t form, const void* ws_, int64
   const int64_t bn = 128 * nsub;
   P.bpack = ws;
   P.bp_kbs = (A->host.cols + 15) / 16;
-  P.aval = A->d_aval[form];
-  P.panels = A->pc[plan_class(form)].d_panels;
-  P.stages = A->pc[plan_class(form)].d_stages;
-  P.row_map = A->pc[plan_class(form)].d_row_map;
+  const int cls = plan_class(form, nsub);
+  P.aval = cls == 3 ? A->d_aval_wide[form == SMAT_FORM_BF16 ? 1 : 0] : A->d_aval[form];
+  P.panels = A->pc[cls].d_panels;
+  P.stages = A->pc[cls].d_stages;
+  P.row_map = A->pc[cls].d_row_map;
   P.C = C;
   P.ldc = ldc;
   P.counters = reinterpret_cast<int32_t*>(ws + wl.counters + 16);  // after the next-item counter
   P.slabs = reinterpret_cast<float*>(ws + wl.slabs);
   P.N = (int32_t)N;
   P.n_tiles = (int32_t)((N + bn - 1) / bn);
-  P.nbr = A->pc[plan_class(form)].plan.n_panels * A->pc[plan_class(form)].plan.R;  // plan rows (slots)
+  P.nbr = A->pc[cls].plan.n_panels * A->pc[cls].plan.R;  // plan rows (slots)
   P.c_f16 = c_dtype == SMAT_F16;
   // instruction descriptor (kind::f16): FP32 accumulator, FP16 (0) or BF16 (1)
   // operands, both K-major, M = 128; the kernel adds N per MMA group
@@ -647,7 +674,7 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   const int nsub = pick_nsub(A, N, kind);
   const int bh = hb.bh, R = A->R;
   if (!tc_variant_supported(bh, R, nsub, kind)) return fail(SMAT_ERR_UNSUPPORTED, "no kernel variant");
-  const Sched& sc = A->pc[plan_class(form)].sched[nsub];
+  const Sched& sc = A->pc[plan_class(form, nsub)].sched[nsub];
   SpmmArgs args;
   std::memset(&args, 0, sizeof(args));
   const WsLayout wl = ws_layout(A, form, N);
@@ -658,6 +685,7 @@ smat_status smat_spmm_packed(const smat_bcsr* A, int32_t form, const void* packe
   args.err = A->d_err;
   args.wait_ns = A->wait_ns;
   args.stall_stage = const_cast<smat_bcsr*>(A)->stall.exchange(0);
+  args.depth = A->depth;
   uint8_t* ctr = static_cast<uint8_t*>(const_cast<void*>(packed_b)) + wl.counters;
   args.next_item = reinterpret_cast<int32_t*>(ctr);
   {

@@ -140,7 +140,7 @@ smat_status smat_group_create(const smat_problem* probs, int32_t count, smat_gro
     std::vector<const Plan*> plans;
     std::vector<int32_t> bhs;
     for (int32_t i : members) {
-      plans.push_back(&probs[i].A->pc[plan_class_of_kind(kind)].plan);
+      plans.push_back(&probs[i].A->pc[plan_class_of_kind(kind, nsub)].plan);
       bhs.push_back(probs[i].A->host.bh);
     }
     const int workers = std::max(1, g->num_sms * tc_ctas_per_sm(bh, std::get<1>(kv.first), nsub, kind));

@@ -176,6 +176,9 @@ struct SmatBcsrBody {
   // blocks in consumption order (hi, then lo for the split form) and the
   // stage header
   uint8_t* d_aval[4] = {nullptr, nullptr, nullptr, nullptr};
+  // the same for the 256-column plan (class 3): FP16, BF16
+  uint8_t* d_aval_wide[2] = {nullptr, nullptr};
+  int32_t depth = 0;                 // pipeline stages in flight (0: all that fit)
   // FP8 form, BCSR block order: e4m3 codes and per-block scales (for export)
   std::vector<uint8_t> fp8_q;
   std::vector<float> fp8_scale;
@@ -202,10 +205,12 @@ namespace smat {
 // Kernel kind of an arithmetic form, its plan class, and the N-tile width
 // (128 * nsub) used for N.
 int kind_of(int32_t form);
-inline int plan_class(int32_t form) {
-  return form == SMAT_FORM_SPLIT_BF16 ? 1 : (form == SMAT_FORM_FP8 ? 2 : 0);
+inline int plan_class(int32_t form, int nsub = 1) {
+  return form == SMAT_FORM_SPLIT_BF16 ? 1 : (form == SMAT_FORM_FP8 ? 2 : (nsub == 2 ? 3 : 0));
 }
-inline int plan_class_of_kind(int kind) { return kind == TC_KIND_SPLIT ? 1 : (kind == TC_KIND_FP8 ? 2 : 0); }
+inline int plan_class_of_kind(int kind, int nsub = 1) {
+  return kind == TC_KIND_SPLIT ? 1 : (kind == TC_KIND_FP8 ? 2 : (nsub == 2 ? 3 : 0));
+}
 // Block rows per panel when the caller leaves it to the library: 256 rows
 // (16 blocks of 16 rows, 8 of 32), two TMEM accumulator buffers of 256
 // columns; panels costing more than kDefaultSplitFrac of the average CTA
@@ -254,6 +259,8 @@ struct TuneKey {
 struct TuneVal {
   int32_t panel_rows = 16;
   float split_frac = 1.0f;
+  int32_t n_tile_cols = 128;
+  int32_t depth = 0;
   double ms = 0.0;
 };
 bool tune_key_of(const HostBcsr& b, int kind, int64_t N, TuneKey& key);

@@ -82,7 +82,8 @@ template <int BH, int R, int NSUB, int KIND>
 struct Cfg {
   static constexpr int BN = 128 * NSUB;                   // C columns per tile
   static constexpr int NOPS = (KIND == KIND_SPLIT) ? 2 : 1;
-  static constexpr int CLS = KIND == KIND_SPLIT ? 1 : (KIND == KIND_FP8 ? 2 : 0);  // plan class (stage shape)
+  // plan class (stage shape): 256-column B tiles (NSUB 2) halve the tiles per stage
+  static constexpr int CLS = KIND == KIND_SPLIT ? 1 : (KIND == KIND_FP8 ? 2 : (NSUB == 2 ? 3 : 0));
   static constexpr int SB = stage_rows(CLS) / BH;         // A blocks per stage (at most)
   static constexpr int ST = stage_tiles(CLS);             // B tiles per stage (at most)
   static constexpr int HDRMAX = stage_hdr_max(SB);
@@ -116,10 +117,13 @@ struct Cfg {
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0,
                 "TMEM allocation must be a power of two in [32, 512]");
   static_assert(BH == 16 || BH == 32, "block height");
-  static_assert(NSUB == 1, "packed B is [column tile][k-block]: a stage tile is one 128-column tile");
+  static_assert(NSUB == 1 || (NSUB == 2 && KIND == KIND_PLAIN), "256-column tiles: plain form only");
   static_assert(R <= 32, "slot field is 5 bits");
   static_assert(SB <= kMaxStageBlocks, "position field is 5 bits");
-  static_assert(ST + 1 <= 2 * NPROD && ST <= kMaxStageTiles, "1 + ST copies per stage, at most two per copy warp");
+  // a stage tile of NSUB 128-column subtiles is NSUB copies (packed B is
+  // [128-column tile][k-block]: the subtiles are not adjacent)
+  static_assert(ST * NSUB + 1 <= 2 * NPROD && ST <= kMaxStageTiles,
+                "1 + ST * NSUB copies per stage, at most two per copy warp");
   static_assert(NS_FIT >= 2, "two stages must fit");
   static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
   static_assert(!FP8 || (BH == 16 && NSUB == 1), "FP8 form: 16 x 16 blocks, 128-column tiles");
@@ -235,6 +239,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t lim = args.wait_ns ? args.wait_ns : kWaitTimeoutNs;
+  // stage slots in use (the pipeline depth): all that fit, or fewer when the
+  // launch asks
+  const uint32_t nsr = (args.depth >= 2 && args.depth < C::NS) ? (uint32_t)args.depth : (uint32_t)C::NS;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < C::NS; i++) {
@@ -290,8 +297,8 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       const int n_tiles = P.n_tiles;
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
         for (int c = wi.s0; c < wi.s1; ++c, ++ci) {
-          const uint32_t s = ci % C::NS;
-          if (!warp_wait(smem_u32(&full[s]), (ci / C::NS) & 1, lane, abort_flag, err, ERR_CONV, false, lim)) {
+          const uint32_t s = ci % nsr;
+          if (!warp_wait(smem_u32(&full[s]), (ci / nsr) & 1, lane, abort_flag, err, ERR_CONV, false, lim)) {
             ok = false;
             break;
           }
@@ -401,18 +408,21 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               hword = C::FP8 ? (int)C::OFF_STG + r1.x * 256 + fp8_scale_bytes(r1.x) : r1.x * (int)(C::ABLK * C::NOPS);
               total = bytes1 + ntl * (int)C::TILEB;
             }
-            // B copies, one per tile (several copies in flight land sooner
-            // than one long copy of adjacent tiles): copy j >= 1 brings tile
-            // j - 1, this warp's are tiles j0 - 1 and j0 + NPROD - 1
-            if (j0 >= 1 && j0 <= ntl) {
-              off1 = ((int64_t)bcol * p_kbs + rp->kb[j0 - 1]) * (4096 * C::NOPS);
-              bytes1 = (int)C::TILEB;
-              dst1 = j0 - 1;
+            // B copies, one per 128-column subtile (several copies in flight
+            // land sooner than one long copy of adjacent tiles): copy c >= 1
+            // brings subtile (c - 1) % NSUB of tile (c - 1) / NSUB; this
+            // warp's are copies j0 and j0 + NPROD
+            if (j0 >= 1 && j0 <= ntl * NSUB) {
+              const int t = (j0 - 1) / NSUB, sub = (j0 - 1) % NSUB;
+              off1 = ((int64_t)(bcol + sub) * p_kbs + rp->kb[t]) * (4096 * C::NOPS);
+              bytes1 = 4096 * C::NOPS;
+              dst1 = t * (int)C::TILEB + sub * 4096 * C::NOPS;
             }
-            if (j0 + C::NPROD <= ntl) {
-              off2 = ((int64_t)bcol * p_kbs + rp->kb[j0 + C::NPROD - 1]) * (4096 * C::NOPS);
-              bytes2 = (int)C::TILEB;
-              dst2 = j0 + C::NPROD - 1;
+            if (j0 + C::NPROD <= ntl * NSUB) {
+              const int t = (j0 + C::NPROD - 1) / NSUB, sub = (j0 + C::NPROD - 1) % NSUB;
+              off2 = ((int64_t)(bcol + sub) * p_kbs + rp->kb[t]) * (4096 * C::NOPS);
+              bytes2 = 4096 * C::NOPS;
+              dst2 = t * (int)C::TILEB + sub * 4096 * C::NOPS;
             }
           }
           for (int i = 0; i < cnt; ++i, ++ci) {
@@ -425,13 +435,13 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
             const int tot = shfl_i(total, i);
             const int hw = shfl_i(hword, i);
             const int j = copy_of(pw, ci, C::NPROD);
-            const uint32_t s = ci % C::NS;
+            const uint32_t s = ci % nsr;
             // The warp with copy 0 waits for the slot and passes its verdict
             // to the other copy warps through a named barrier (blocked warps
             // take no issue slots); so all copy warps move stage by stage and
             // none can run a ring ahead and overwrite a stage still in use.
             if (j == 0 && lane == 0)
-              stage_ok[s] = wait_phase(smem_u32(&empty[s]), ((ci / C::NS) & 1) ^ 1, abort_flag, err, ERR_PROD_A, lim) ? 1 : 0;
+              stage_ok[s] = wait_phase(smem_u32(&empty[s]), ((ci / nsr) & 1) ^ 1, abort_flag, err, ERR_PROD_A, lim) ? 1 : 0;
             named_bar_sync(1, 32 * C::NPROD);
             int good = 1;
             if (lane == 0) {
@@ -445,9 +455,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
                   mbar_arrive_expect_tx(fb, (uint32_t)tot);
                   bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), p_aval + o1, (uint32_t)b1, fb, pol_a);
                 } else {
-                  bulk_load_hint(st + C::OFF_B + d1 * C::TILEB, p_bpack + o1, (uint32_t)b1, fb, pol_b);
+                  bulk_load_hint(st + C::OFF_B + d1, p_bpack + o1, (uint32_t)b1, fb, pol_b);
                 }
-                if (b2 != 0) bulk_load_hint(st + C::OFF_B + d2 * C::TILEB, p_bpack + o2, (uint32_t)b2, fb, pol_b);
+                if (b2 != 0) bulk_load_hint(st + C::OFF_B + d2, p_bpack + o2, (uint32_t)b2, fb, pol_b);
                 if (b1 != 0 || b2 != 0) last_mine = ci;
               } else {
                 good = 0;
@@ -465,9 +475,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     if (!ok && lane == 0 && last_mine != 0xffffffffu) {
       // wait for this warp's own copies still in flight: they can only be in
       // the last NS stages it copied into
-      const uint32_t lo = last_mine + 1 > (uint32_t)C::NS ? last_mine + 1 - C::NS : 0;
+      const uint32_t lo = last_mine + 1 > nsr ? last_mine + 1 - nsr : 0;
       for (uint32_t k = lo; k <= last_mine; ++k)
-        mbar_wait_drain(smem_u32(&full[k % C::NS]), (k / C::NS) & 1, err, lim);
+        mbar_wait_drain(smem_u32(&full[k % nsr]), (k / nsr) & 1, err, lim);
     }
   } else if (warp < C::NMMA) {
     if (lane == 0) {
@@ -502,7 +512,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
           }
           tc_fence_after();
           for (int c = 0; c < nstages; ++c, ++ci) {
-            const uint32_t s = slot_s;  // == ci % NS, kept incrementally
+            const uint32_t s = slot_s;  // == ci % nsr, kept incrementally
             if (stall != 0u && ci + 1 == stall) {
               // test stall: nothing arrives on this barrier, so the wait runs
               // into its limit and the CTA aborts
@@ -544,7 +554,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
               issued = true;
             }
             umma_commit(smem_u32(&empty[s]));
-            if (++slot_s == (uint32_t)C::NS) {
+            if (++slot_s == nsr) {
               slot_s = 0;
               phase_s ^= 1u;
             }
@@ -826,6 +836,8 @@ static int ctas_per_sm_one() {
   X(16, 4, 1, 0)            \
   X(16, 8, 1, 0)            \
   X(16, 16, 1, 0)           \
+  X(16, 4, 2, 0)            \
+  X(16, 8, 2, 0)            \
   X(32, 4, 1, 0)            \
   X(32, 8, 1, 0)            \
   X(16, 4, 1, 1)            \

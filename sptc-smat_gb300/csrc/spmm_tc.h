@@ -11,19 +11,20 @@ namespace smat {
 
 // A pipeline STAGE carries up to stage_rows(cls) / bh A blocks of one panel
 // (in the order the kernel consumes them), up to stage_tiles(cls) packed B
-// tiles those blocks need, and the stage's MMA list. There are three stage
+// tiles those blocks need, and the stage's MMA list. There are four stage
 // shapes ("plan classes"), each the largest that still leaves three stages
 // in flight in shared memory: class 0 for the FP16 and BF16 forms (28
 // blocks of 16 rows and 14 B tiles: 14 KB of A and 56 KB of B), class 1
 // for the split form, whose stages hold hi and lo copies of everything (14
 // blocks and 7 tiles: the same bytes), class 2 for the FP8 form, whose
 // stages also stage the e4m3 blocks before conversion (24 blocks, 12
-// tiles).
-constexpr int kPlanClasses = 3;
+// tiles), class 3 for the FP16 and BF16 forms with 256-column B tiles (N >
+// 128 in one pass over A: 14 blocks and 7 tiles of 8 KB).
+constexpr int kPlanClasses = 4;
 constexpr int kMaxStageTiles = 16;   // StageRec::kb capacity (a copy warp issues at most two copies)
 constexpr int kMaxStageBlocks = 31;  // the entry's position field has 5 bits
-__host__ __device__ constexpr int stage_rows(int cls) { return cls == 0 ? 448 : (cls == 1 ? 224 : 384); }
-__host__ __device__ constexpr int stage_tiles(int cls) { return cls == 0 ? 14 : (cls == 1 ? 7 : 12); }
+__host__ __device__ constexpr int stage_rows(int cls) { return cls == 0 ? 448 : (cls == 2 ? 384 : 224); }
+__host__ __device__ constexpr int stage_tiles(int cls) { return cls == 0 ? 14 : (cls == 2 ? 12 : 7); }
 constexpr int kMmaWarps = 4;      // MMA-issuing warps; each owns a quarter of a panel's TMEM slots
 constexpr int kMinCutBlocks = 16; // a block row is cut over the issuing warps only from this many blocks
 constexpr int kMaxGroupN = 256;   // widest tcgen05.mma N (kind::f16, M = 128)
@@ -123,7 +124,9 @@ struct ProblemDesc {
 // free first takes the largest item left (the counter is zero at launch).
 // wait_ns bounds every device-side wait (0: 4 s); stall_stage k > 0 makes
 // the first MMA-issuing thread of CTA 0 wait, before its k-th stage, on a
-// barrier nothing arrives at (a test of the bounded-wait error path).
+// barrier nothing arrives at (a test of the bounded-wait error path);
+// depth >= 2 caps the stage slots in flight (the pipeline depth; 0: all
+// that fit in shared memory).
 struct SpmmArgs {
   ProblemDesc one;
   const ProblemDesc* probs;
@@ -134,6 +137,8 @@ struct SpmmArgs {
   int32_t n_items;
   int32_t stall_stage;
   uint64_t wait_ns;
+  int32_t depth;
+  int32_t pad_;
 };
 
 // Kernel kinds: 0 plain (FP16 or BF16 A and B), 1 split hi+lo BF16, 2 FP8 A

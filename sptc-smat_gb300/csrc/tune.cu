@@ -1,11 +1,15 @@
 // tune.cu — the SpMM autotuner.
 //
 // smat_autotune measures the launch shapes the library offers for a matrix
-// (block rows per panel R, and how far heavy panels are split across CTAs)
-// on the device, with CUDA events, and keeps the fastest in a process-wide
-// cache keyed on the matrix's block-density statistics: blocks per block
-// row and blocks per B tile inside a 16-row panel (how much one B tile is
-// reused), both log2-bucketed, plus the N-tile count and the kernel kind.
+// on the device, with CUDA events: block rows per panel R (the rows one CTA
+// work item covers), how far heavy panels are split across CTAs, the N-tile
+// width (128 columns per pass over A, or 256 when N > 128 and R <= 8, where
+// the two accumulator buffers still fit tensor memory) and then, for the best
+// of those, the pipeline depth (stages in flight). It keeps the fastest in a
+// process-wide cache keyed on the matrix's block-density statistics: blocks
+// per block row and blocks per B tile inside a 16-row panel (how much one B
+// tile is reused), both log2-bucketed, plus the N-tile count and the kernel
+// kind.
 // smat_bcsr_create with panel_rows = 0 looks its matrix up in that cache, so
 // one tuning run serves every matrix with similar statistics.
 #include <cuda_runtime.h>
@@ -87,6 +91,8 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
   if (tune_lookup(key, cached)) {
     out->panel_rows = cached.panel_rows;
     out->split_frac = cached.split_frac;
+    out->n_tile_cols = cached.n_tile_cols;
+    out->pipeline_depth = cached.depth;
     out->ms = cached.ms;
     out->cached = 1;
     return SMAT_OK;
@@ -110,51 +116,81 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
   TuneVal best;
   best.ms = INFINITY;
   double ms_default = 0.0;
+  int candidates = 0;
+  // one candidate: build the handle, 3 warm-up and 8 timed SpMMs; < 0 when
+  // the shape is not offered for this form, NaN on a failure
+  auto measure = [&](int R, float f, int ntc, int depth) -> double {
+    smat_bcsr_opts oc = o;
+    oc.panel_rows = R;
+    oc.split_frac = f;
+    oc.n_tile_cols = ntc;
+    oc.pipeline_depth = depth;
+    oc.forms = 1u << form;
+    smat_bcsr* h = nullptr;
+    if (smat_bcsr_create(A, &oc, &h) != SMAT_OK) return -1.0;  // shape not offered for this form
+    size_t need = 0;
+    smat_spmm_workspace_size(h, form, SMAT_F32, N, &need);
+    if (need > wbytes) {
+      cudaFree(dW);
+      dW = nullptr;
+      wbytes = 0;
+      if (cudaMalloc(&dW, need) != cudaSuccess) {
+        smat_bcsr_destroy(h);
+        return NAN;
+      }
+      wbytes = need;
+    }
+    float ms = 0.0f;
+    bool run_ok = true;
+    for (int i = 0; i < 3 && run_ok; i++)
+      run_ok = smat_spmm(h, form, dB, SMAT_F32, SMAT_ROW_MAJOR, N, dC, SMAT_F32, N, N, dW, wbytes, s) == SMAT_OK;
+    constexpr int kReps = 8;
+    run_ok = run_ok && cudaEventRecord(e0, s) == cudaSuccess;
+    for (int i = 0; i < kReps && run_ok; i++)
+      run_ok = smat_spmm(h, form, dB, SMAT_F32, SMAT_ROW_MAJOR, N, dC, SMAT_F32, N, N, dW, wbytes, s) == SMAT_OK;
+    run_ok = run_ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+             cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && smat_bcsr_check_device_error(h) == SMAT_OK;
+    smat_bcsr_destroy(h);
+    if (!run_ok) return NAN;
+    candidates++;
+    return ms / kReps;
+  };
+  auto consider = [&](double t, int R, float f, int ntc, int depth) {
+    if (t >= 0.0 && t < best.ms) {
+      best.ms = t;
+      best.panel_rows = R;
+      best.split_frac = f;
+      best.n_tile_cols = ntc;
+      best.depth = depth;
+    }
+  };
+  // panel height x splitting threshold x N-tile width
   for (int R : Rs) {
     for (float f : fracs) {
-      if (!ok) break;
-      smat_bcsr_opts oc = o;
-      oc.panel_rows = R;
-      oc.split_frac = f;
-      oc.forms = 1u << form;
-      smat_bcsr* h = nullptr;
-      if (smat_bcsr_create(A, &oc, &h) != SMAT_OK) continue;  // shape not offered for this form
-      size_t need = 0;
-      smat_spmm_workspace_size(h, form, SMAT_F32, N, &need);
-      if (need > wbytes) {
-        cudaFree(dW);
-        dW = nullptr;
-        wbytes = 0;
-        if (cudaMalloc(&dW, need) != cudaSuccess) {
-          smat_bcsr_destroy(h);
+      for (int ntc : {128, 256}) {
+        if (!ok) break;
+        if (ntc == 256 && (N <= 128 || !tc_variant_supported(bh, R, 2, kind_of(form)))) continue;
+        const double t = measure(R, f, ntc, 0);
+        if (std::isnan(t)) {
           ok = false;
           break;
         }
-        wbytes = need;
+        if (R == default_panel_rows(bh) && f == (float)kDefaultSplitFrac && ntc == 128) ms_default = t;
+        consider(t, R, f, ntc, 0);
       }
-      float ms = 0.0f;
-      bool run_ok = true;
-      for (int i = 0; i < 3 && run_ok; i++)
-        run_ok = smat_spmm(h, form, dB, SMAT_F32, SMAT_ROW_MAJOR, N, dC, SMAT_F32, N, N, dW, wbytes, s) == SMAT_OK;
-      constexpr int kReps = 8;
-      run_ok = run_ok && cudaEventRecord(e0, s) == cudaSuccess;
-      for (int i = 0; i < kReps && run_ok; i++)
-        run_ok = smat_spmm(h, form, dB, SMAT_F32, SMAT_ROW_MAJOR, N, dC, SMAT_F32, N, N, dW, wbytes, s) == SMAT_OK;
-      run_ok = run_ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
-               cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
-               smat_bcsr_check_device_error(h) == SMAT_OK;
-      smat_bcsr_destroy(h);
-      if (!run_ok) {
+    }
+  }
+  // pipeline depth of the best shape: 0 (every stage slot that fits in
+  // shared memory: 3 for every stage shape offered) against 2
+  if (ok && std::isfinite(best.ms)) {
+    const TuneVal b0 = best;
+    for (int depth : {2}) {
+      const double t = measure(b0.panel_rows, b0.split_frac, b0.n_tile_cols, depth);
+      if (std::isnan(t)) {
         ok = false;
         break;
       }
-      const double t = ms / kReps;
-      if (R == default_panel_rows(bh) && f == (float)kDefaultSplitFrac) ms_default = t;
-      if (t < best.ms) {
-        best.ms = t;
-        best.panel_rows = R;
-        best.split_frac = f;
-      }
+      consider(t, b0.panel_rows, b0.split_frac, b0.n_tile_cols, depth);
     }
   }
   cudaFree(dB);
@@ -168,9 +204,12 @@ smat_status smat_autotune(const smat_csr* A, const smat_bcsr_opts* opts, int32_t
   tune_store(key, best);
   out->panel_rows = best.panel_rows;
   out->split_frac = best.split_frac;
+  out->n_tile_cols = best.n_tile_cols;
+  out->pipeline_depth = best.depth;
   out->ms = best.ms;
   out->ms_default = ms_default;
   out->cached = 0;
+  out->candidates = candidates;
   return SMAT_OK;
 }
 

@@ -234,13 +234,16 @@ class Bcsr:
     """A BCSR matrix resident on one GPU (the reference's ``SparseMatrix``)."""
 
     def __init__(self, csr: Csr, block=(16, 16), forms=(FORM_F16,), row_perm=None, panel_rows: int = 0,
-                 device: int = 0, use_24: bool = False, split_frac: float = 0.0, col_perm=None):
+                 device: int = 0, use_24: bool = False, split_frac: float = 0.0, col_perm=None,
+                 n_tile_cols: int = 0, pipeline_depth: int = 0):
         o = BcsrOpts()
         o.block_rows, o.block_cols = block
         o.forms = 0
         for f in forms:
             o.forms |= 1 << f
         o.use_24 = int(use_24)          # True: every exact-2:4 block; k > 1: units of >= k such blocks
+        o.n_tile_cols = n_tile_cols
+        o.pipeline_depth = pipeline_depth
         self._perm = None if row_perm is None else np.ascontiguousarray(row_perm, np.int64)
         o.row_perm = None if self._perm is None else self._perm.ctypes.data
         o.device = device
@@ -373,7 +376,8 @@ def autotune(csr: Csr, form: int = FORM_F16, N: int = 128, block=(16, 16), row_p
     s = csr.struct()
     check(lib().smat_autotune(C.byref(s), C.byref(o), form, N, C.byref(r)))
     return {"panel_rows": r.panel_rows, "split_frac": r.split_frac, "ms": r.ms, "ms_default": r.ms_default,
-            "cached": bool(r.cached)}
+            "cached": bool(r.cached), "n_tile_cols": r.n_tile_cols, "pipeline_depth": r.pipeline_depth,
+            "candidates": r.candidates}
 
 
 def features(csr: Csr, device: int = 0) -> np.ndarray:

@@ -32,7 +32,8 @@ class CsrStruct(C.Structure):
 class BcsrOpts(C.Structure):
     _fields_ = [("block_rows", C.c_int32), ("block_cols", C.c_int32), ("forms", C.c_uint32),
                 ("use_24", C.c_int32), ("row_perm", C.c_void_p), ("device", C.c_int32),
-                ("panel_rows", C.c_int32), ("split_frac", C.c_float), ("col_perm", C.c_void_p)]
+                ("panel_rows", C.c_int32), ("split_frac", C.c_float), ("col_perm", C.c_void_p),
+                ("n_tile_cols", C.c_int32), ("pipeline_depth", C.c_int32)]
 
 
 class CsrFile(C.Structure):
@@ -47,7 +48,8 @@ class Problem(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("panel_rows", C.c_int32), ("split_frac", C.c_float), ("ms", C.c_double),
-                ("ms_default", C.c_double), ("cached", C.c_int32)]
+                ("ms_default", C.c_double), ("cached", C.c_int32), ("n_tile_cols", C.c_int32),
+                ("pipeline_depth", C.c_int32), ("candidates", C.c_int32)]
 
 
 class BcsrInfo(C.Structure):
@@ -55,7 +57,7 @@ class BcsrInfo(C.Structure):
                 ("cols_padded", C.c_int64), ("nnz", C.c_int64), ("nnzb", C.c_int64),
                 ("n_blocks_24", C.c_int64), ("block_rows", C.c_int32), ("block_cols", C.c_int32),
                 ("panel_rows", C.c_int32), ("n_panels", C.c_int32), ("n_union_cols", C.c_int64),
-                ("fill", C.c_double)]
+                ("fill", C.c_double), ("n_tile_cols", C.c_int32), ("pipeline_depth", C.c_int32)]
 
 
 class ReorderStats(C.Structure):
