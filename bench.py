@@ -561,6 +561,109 @@ def run_forms(args):
         Mt.close()
 
 
+def _cusparse_blocked_ell(A, perm, Bh, N, dev, steps, warmup):
+    """cuSPARSE Blocked-ELL SpMM (cusparseSpMM, CUSPARSE_SPMM_BLOCKED_ELL_ALG1)
+    on the reordered matrix's 16x16 blocks, every block row padded to the
+    widest one, through ctypes; returns (ms, C in the reordered row order,
+    ELL bytes, stored blocks) or raises with the reason."""
+    import ctypes
+    import glob
+
+    import torch
+
+    import smat
+    cs = None
+    for c in sorted(glob.glob("/usr/local/cuda/lib64/libcusparse.so*")) + ["libcusparse.so"]:
+        try:
+            cs = ctypes.CDLL(c)
+            break
+        except OSError:
+            continue
+    if cs is None:
+        raise RuntimeError("libcusparse not found")
+    M = smat.Bcsr(A, row_perm=perm)
+    rp, ci, vals, _ = M.export()
+    nbr = len(rp) - 1
+    M.close()
+    bpr = np.diff(rp)
+    width = int(bpr.max())
+    rows, cols = nbr * 16, int(A.cols + 15) // 16 * 16
+    # block (i, j) of the padded grid: the j-th block of block row i
+    br = np.repeat(np.arange(nbr), bpr)
+    j = np.arange(rp[-1]) - np.repeat(rp[:-1], bpr)
+    col_ind = np.full((nbr, width), -1, np.int32)
+    col_ind[br, j] = ci // 16
+    V = torch.zeros((nbr, width, 16, 16), dtype=torch.float16, device=dev)
+    V[torch.from_numpy(br).to(dev), torch.from_numpy(j).to(dev)] = torch.from_numpy(vals).to(dev)
+    ell_val = V.permute(0, 2, 1, 3).contiguous()            # rows x (width * 16), row-major
+    del V
+    d_ind = torch.from_numpy(col_ind).to(dev)
+    Bd = torch.zeros((cols, N), dtype=torch.float16, device=dev)
+    Bd[: A.cols] = torch.from_numpy(Bh).to(dev)
+    Bc = Bd.t().contiguous()                                 # column-major K x N (ld = K)
+    Cc = torch.zeros((N, rows), dtype=torch.float32, device=dev)  # column-major M x N (ld = M)
+    vp = ctypes.c_void_p
+    i64 = ctypes.c_int64
+    cs.cusparseCreate.argtypes = [ctypes.POINTER(vp)]
+    cs.cusparseDestroy.argtypes = [vp]
+    cs.cusparseCreateBlockedEll.argtypes = [ctypes.POINTER(vp), i64, i64, i64, i64, vp, vp, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int]
+    cs.cusparseCreateDnMat.argtypes = [ctypes.POINTER(vp), i64, i64, i64, vp, ctypes.c_int, ctypes.c_int]
+    cs.cusparseDestroySpMat.argtypes = [vp]
+    cs.cusparseDestroyDnMat.argtypes = [vp]
+    cs.cusparseSpMM_bufferSize.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_int,
+                                            ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+    cs.cusparseSpMM.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp]
+    R16F, R32F, IDX32, BASE0, ORDER_COL, ALG = 2, 0, 2, 0, 1, 13   # cuda_runtime / cusparse.h enum values
+    h = vp()
+    st = cs.cusparseCreate(ctypes.byref(h))
+    if st:
+        raise RuntimeError(f"cusparseCreate: status {st}")
+    mA, mB, mC = vp(), vp(), vp()
+    try:
+        st = cs.cusparseCreateBlockedEll(ctypes.byref(mA), rows, cols, 16, width * 16, vp(d_ind.data_ptr()),
+                                         vp(ell_val.data_ptr()), IDX32, BASE0, R16F)
+        st = st or cs.cusparseCreateDnMat(ctypes.byref(mB), cols, N, cols, vp(Bc.data_ptr()), R16F, ORDER_COL)
+        st = st or cs.cusparseCreateDnMat(ctypes.byref(mC), rows, N, rows, vp(Cc.data_ptr()), R32F, ORDER_COL)
+        if st:
+            raise RuntimeError(f"descriptor creation: status {st}")
+        alpha, beta = ctypes.c_float(1.0), ctypes.c_float(0.0)
+        pa, pb = ctypes.cast(ctypes.byref(alpha), vp), ctypes.cast(ctypes.byref(beta), vp)
+        nbytes = ctypes.c_size_t(0)
+        st = cs.cusparseSpMM_bufferSize(h, 0, 0, pa, mA, mB, pb, mC, R32F, ALG, ctypes.byref(nbytes))
+        if st:
+            raise RuntimeError(f"cusparseSpMM_bufferSize: status {st}")
+        buf = torch.empty(max(int(nbytes.value), 16), dtype=torch.uint8, device=dev)
+
+        def call():
+            r = cs.cusparseSpMM(h, 0, 0, pa, mA, mB, pb, mC, R32F, ALG, vp(buf.data_ptr()))
+            if r:
+                raise RuntimeError(f"cusparseSpMM: status {r}")
+
+        call()
+        torch.cuda.synchronize(dev)
+        for _ in range(max(warmup, 3)):
+            call()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            call()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        out = Cc.t()[: A.rows].double().cpu().numpy()
+    finally:
+        if mA:
+            cs.cusparseDestroySpMat(mA)
+        if mB:
+            cs.cusparseDestroyDnMat(mB)
+        if mC:
+            cs.cusparseDestroyDnMat(mC)
+        cs.cusparseDestroy(h)
+    return ms, out, ell_val.numel() * 2 + d_ind.numel() * 4, nbr * width
+
+
 def run_libraries(args):
     """Library comparison on the R-MAT workload: cuSPARSE CSR SpMM (through
     torch.sparse.mm) on the same A and B as the headline line, one JSON line
@@ -610,6 +713,22 @@ def run_libraries(args):
                            "step": "one torch.sparse.mm call"}}),
               flush=True)
         del S, B, out
+    # Blocked-ELL, the reference's other cuSPARSE comparison (cuda_utilities.cpp:1497-1654)
+    name = "cuSPARSE Blocked-ELL SpMM, 16x16 blocks of the reordered matrix, FP16 values and B, FP32 C"
+    try:
+        _, perm = build_matrix()
+        ms, outp, ell_bytes, stored = _cusparse_blocked_ell(A, perm, Bh, N, dev, args.steps, args.warmup)
+        err = float(np.linalg.norm(outp - ref[perm]) / nrm)
+        print(json.dumps({"metric": METRIC, "library": name, "value": useful / (ms * 1e-3) / 1e12,
+                          "unit": "TFLOP/s", "ms_per_step": ms, "rel_err_vs_fp64": err, "steps": args.steps,
+                          "warmup": args.warmup, "higher_is_better": True, "data": "synthetic",
+                          "config": {k: WORKLOAD[k] for k in ("workload", "generator", "N", "B", "C")} |
+                          {"nnz": A.nnz, "A": "Blocked-ELL, every block row padded to the widest "
+                           f"({stored} stored blocks, {ell_bytes / 1e9:.2f} GB)",
+                           "step": "one cusparseSpMM call (CUSPARSE_SPMM_BLOCKED_ELL_ALG1)"}}), flush=True)
+    except Exception as e:  # the library or the format unavailable on this machine
+        print(json.dumps({"metric": METRIC, "library": name, "unavailable": str(e).splitlines()[0][:200]}),
+              flush=True)
 
 
 PRUNED24_WORKLOAD = {

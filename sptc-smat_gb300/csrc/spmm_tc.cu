@@ -109,7 +109,7 @@ struct Cfg {
   static constexpr int NMMA = kMmaWarps;                  // MMA-issuing warps
   static constexpr int NPROD = 8;                         // copy warps
   static constexpr int NCONV = FP8 ? 4 : 0;               // FP8 converter warps (16..19)
-  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? NS : 0) + 2 * kItemRing + 1);
+  static constexpr uint32_t SMEM_BARS = 8 * (2 * NS + 4 + NMMA + (FP8 ? 2 * NS : 0) + 2 * kItemRing + 1);
   // then the TMEM address, the abort flag, stage_ok[NS], the item ring and
   // the copy warps' current item
   static constexpr uint32_t SMEM_BYTES = 1024 + NS * STAGE + SMEM_BARS + 8 + 4 * (NS + kItemRing + 1);
@@ -227,7 +227,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
   uint64_t* accempty = accfull + 2;
   uint64_t* drainbar = accempty + 2;
   uint64_t* conv = drainbar + C::NMMA;  // FP8: the stage's A blocks are converted
-  uint64_t* itemfull = conv + (C::FP8 ? C::NS : 0);  // [kItemRing] an item index is in the ring
+  // FP8: the stage's A copy landed (the converters start on it while the B
+  // tiles are still landing on full[])
+  uint64_t* afull = conv + (C::FP8 ? C::NS : 0);
+  uint64_t* itemfull = afull + (C::FP8 ? C::NS : 0);  // [kItemRing] an item index is in the ring
   uint64_t* itemempty = itemfull + kItemRing;        // [kItemRing] every role has read it
   uint64_t* stallbar = itemempty + kItemRing;        // nothing arrives here (test stall)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(stallbar + 1);
@@ -254,7 +257,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
     }
     for (int i = 0; i < C::NMMA; i++) mbar_init(smem_u32(&drainbar[i]), 1);
     if (C::FP8)
-      for (int i = 0; i < C::NS; i++) mbar_init(smem_u32(&conv[i]), C::NCONV);
+      for (int i = 0; i < C::NS; i++) {
+        mbar_init(smem_u32(&conv[i]), C::NCONV);
+        mbar_init(smem_u32(&afull[i]), 1);
+      }
     for (int i = 0; i < kItemRing; i++) {
       mbar_init(smem_u32(&itemfull[i]), 1);
       mbar_init(smem_u32(&itemempty[i]), C::NMMA + 4 + C::NCONV);  // lane 0 of every other warp
@@ -298,7 +304,7 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       for (int nt = 0; nt < n_tiles && ok; ++nt) {
         for (int c = wi.s0; c < wi.s1; ++c, ++ci) {
           const uint32_t s = ci % nsr;
-          if (!warp_wait(smem_u32(&full[s]), (ci / nsr) & 1, lane, abort_flag, err, ERR_CONV, false, lim)) {
+          if (!warp_wait(smem_u32(&afull[s]), (ci / nsr) & 1, lane, abort_flag, err, ERR_CONV, false, lim)) {
             ok = false;
             break;
           }
@@ -452,8 +458,17 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
                   // no copy for this warp in this stage
                 } else if (j == 0) {
                   *reinterpret_cast<uint32_t*>(smem + s * C::STAGE + C::OFF_HW) = (uint32_t)hw;
-                  mbar_arrive_expect_tx(fb, (uint32_t)tot);
-                  bulk_load_hint(st + (C::FP8 ? C::OFF_STG : 0u), p_aval + o1, (uint32_t)b1, fb, pol_a);
+                  if (C::FP8) {
+                    // the A region on its own barrier (the converters wait
+                    // for it alone), the B tiles on full[s]
+                    const uint32_t ab = smem_u32(&afull[s]);
+                    mbar_arrive_expect_tx(ab, (uint32_t)b1);
+                    bulk_load_hint(st + C::OFF_STG, p_aval + o1, (uint32_t)b1, ab, pol_a);
+                    mbar_arrive_expect_tx(fb, (uint32_t)(tot - b1));
+                  } else {
+                    mbar_arrive_expect_tx(fb, (uint32_t)tot);
+                    bulk_load_hint(st, p_aval + o1, (uint32_t)b1, fb, pol_a);
+                  }
                 } else {
                   bulk_load_hint(st + C::OFF_B + d1, p_bpack + o1, (uint32_t)b1, fb, pol_b);
                 }
@@ -476,8 +491,10 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
       // wait for this warp's own copies still in flight: they can only be in
       // the last NS stages it copied into
       const uint32_t lo = last_mine + 1 > nsr ? last_mine + 1 - nsr : 0;
-      for (uint32_t k = lo; k <= last_mine; ++k)
+      for (uint32_t k = lo; k <= last_mine; ++k) {
         mbar_wait_drain(smem_u32(&full[k % nsr]), (k / nsr) & 1, err, lim);
+        if (C::FP8) mbar_wait_drain(smem_u32(&afull[k % nsr]), (k / nsr) & 1, err, lim);
+      }
     }
   } else if (warp < C::NMMA) {
     if (lane == 0) {
@@ -521,7 +538,9 @@ __global__ void __launch_bounds__(Cfg<BH, R, NSUB, KIND>::THREADS, 1)
             }
             // the stage's copies landed (complete_tx); the MMA reads shared
             // memory through the async proxy, so no tcgen05 fence is needed
-            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &full[s]), phase_s, abort_flag, err, ERR_MMA_A, lim)) {
+            // (FP8: the converted A blocks, then the B tiles)
+            if (!wait_phase(smem_u32(C::FP8 ? &conv[s] : &full[s]), phase_s, abort_flag, err, ERR_MMA_A, lim) ||
+                (C::FP8 && !wait_phase(smem_u32(&full[s]), phase_s, abort_flag, err, ERR_MMA_B, lim))) {
               ok = false;
               break;
             }
