@@ -164,8 +164,9 @@ smat_status smat_csr_file_free(smat_csr_file* f);
  * identical to the reference's permutation; grouping_out (optional) receives
  * the final grouping vector (the reference's ".g" file content). A column
  * index is "the" column (col_idx); the pattern is used, values are ignored.
- * The scan runs on the host's cores; use_gpu must be 0 (1 returns
- * SMAT_ERR_UNSUPPORTED: there is no device scan). */
+ * use_gpu = 0: the candidate distances of the scan run on the host's cores;
+ * use_gpu != 0: on the current CUDA device, in larger chunks (the seed loop
+ * and its commits stay on the host), with the same result. */
 smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_t row_block,
                          int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
                          int64_t* grouping_out, smat_reorder_stats* stats);

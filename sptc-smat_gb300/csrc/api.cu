@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -324,8 +325,6 @@ smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_
                          int32_t algo, int32_t force_fixed, int32_t use_gpu, int64_t* perm_out,
                          int64_t* grouping_out, smat_reorder_stats* stats) {
   if (!A || !perm_out) return fail(SMAT_ERR_INVALID, "null argument");
-  if (use_gpu)
-    return fail(SMAT_ERR_UNSUPPORTED, "use_gpu: the reorder scan runs on the host's cores only (pass 0)");
   if (A->rows < 0 || !A->row_ptr || (A->nnz > 0 && !A->col_idx))
     return fail(SMAT_ERR_INVALID, "malformed CSR");
   if (col_block < 1 || row_block < 1) return fail(SMAT_ERR_INVALID, "block sizes must be >= 1");
@@ -338,8 +337,18 @@ smat_status smat_reorder(const smat_csr* A, float tau, int32_t col_block, int32_
   std::vector<int64_t> g;
   int64_t comparisons = 0, merges = 0;
   if (algo == 5) {
-    keeper_grouping_host(A->rows, A->row_ptr, A->col_idx, tau, col_block, row_block, g,
-                         comparisons, merges);
+    if (use_gpu) {
+      // candidate distances on the current CUDA device, commit on the host
+      int d = 0;
+      if (cudaGetDevice(&d) != cudaSuccess) return fail(SMAT_ERR_NO_DEVICE, "use_gpu: no CUDA device");
+      std::unique_ptr<KeeperDevice> kd(make_keeper_device(d));
+      if (!kd) return fail(SMAT_ERR_NO_DEVICE, "use_gpu: no CUDA device");
+      if (!keeper_grouping(A->rows, A->row_ptr, A->col_idx, tau, col_block, row_block, g, comparisons, merges,
+                           kd.get()))
+        return fail(SMAT_ERR_CUDA, std::string("use_gpu: ") + kd->error());
+    } else {
+      keeper_grouping_host(A->rows, A->row_ptr, A->col_idx, tau, col_block, row_block, g, comparisons, merges);
+    }
   } else if (algo == 2) {
     // FixedBlocking (blocking.cpp:551-559)
     g.resize(A->rows);

@@ -12,7 +12,9 @@
 // chunk is committed in order up to the first merge, and measuring resumes
 // after it with the grown pattern. Distances are computed on each row's
 // sequence of block-column runs, which is exactly what the reference's
-// distance walk consumes.
+// distance walk consumes. The chunk is measured on the host's cores, or on a
+// GPU (reorder_gpu.cu) with larger chunks; the commit is the same code
+// either way, so both give the same grouping.
 #include <omp.h>
 
 #include <algorithm>
@@ -79,9 +81,9 @@ void merge_rows(std::vector<int64_t>& A, const int64_t* B, int64_t nb, std::vect
 
 }  // namespace
 
-void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* cols32, float tau,
-                          int64_t bs, int64_t max_b, std::vector<int64_t>& grouping,
-                          int64_t& comparisons, int64_t& merges) {
+bool keeper_grouping(int64_t rows, const int64_t* rowptr, const int32_t* cols32, float tau, int64_t bs,
+                     int64_t max_b, std::vector<int64_t>& grouping, int64_t& comparisons, int64_t& merges,
+                     KeeperDevice* dev) {
   const int64_t nnz = rowptr[rows];
   std::vector<int64_t> cols(cols32, cols32 + nnz);
   // per-row run sequences
@@ -96,6 +98,9 @@ void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* co
       run_ptr[r + 1] = (int64_t)runs.size();
     }
   }
+  if (dev && !dev->init(runs, run_ptr)) return false;
+  // chunk sizes: the device pays a round trip per chunk, so it starts larger
+  const int64_t chunk0 = dev ? 2048 : 64, chunk_max = dev ? (int64_t)1 << 18 : (int64_t)1 << 16;
   grouping.assign(rows, -1);
   // `float distances[rows] = {-1}` (GCC VLA initialiser): [-1, 0, 0, ...]
   std::vector<float> distances(rows, 0.0f);
@@ -117,18 +122,22 @@ void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* co
     merged.push_back(i);
     const float di = distances[i];
     int64_t j = i + 1;
-    int64_t chunk = 64;
+    int64_t chunk = chunk0;
     while (j < rows && gsize != max_b) {
       const int64_t j1 = std::min<int64_t>(rows, j + chunk);
       const int64_t* pr = pruns.data();
       const int64_t npr = (int64_t)pruns.size();
       const int64_t g = gsize;
+      if (dev) {
+        if (!dev->fill(pr, npr, g, j, j1, dbuf.data() + j)) return false;
+      } else {
 #pragma omp parallel for schedule(dynamic, 256) if (j1 - j >= 2048)
-      for (int64_t jj = j; jj < j1; jj++) {
-        const float dj = distances[jj];
-        if (di != -1 && dj != -1 && std::fabs(di - dj) > tau) continue;
-        if (grouping[jj] != -1) continue;
-        dbuf[jj] = jaccard_runs(pr, npr, g, runs.data() + run_ptr[jj], run_ptr[jj + 1] - run_ptr[jj]);
+        for (int64_t jj = j; jj < j1; jj++) {
+          const float dj = distances[jj];
+          if (di != -1 && dj != -1 && std::fabs(di - dj) > tau) continue;
+          if (grouping[jj] != -1) continue;
+          dbuf[jj] = jaccard_runs(pr, npr, g, runs.data() + run_ptr[jj], run_ptr[jj + 1] - run_ptr[jj]);
+        }
       }
       int64_t merged_at = -1;
       for (int64_t jj = j; jj < j1; jj++) {
@@ -164,10 +173,10 @@ void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* co
       }
       if (merged_at >= 0) {
         j = merged_at + 1;
-        chunk = 64;
+        chunk = chunk0;
       } else {
         j = j1;
-        chunk = std::min<int64_t>(chunk * 4, 1 << 16);
+        chunk = std::min<int64_t>(chunk * 4, chunk_max);
       }
     }
     if (gsize < max_b) {
@@ -180,6 +189,7 @@ void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* co
     if (gsize == max_b)
       for (int64_t idx : merged) grouping[idx] -= rows;
   }
+  return true;
 }
 
 std::vector<int64_t> permutation_of(const std::vector<int64_t>& grouping) {

@@ -34,10 +34,32 @@ struct ReorderResult {
   int64_t merges = 0;
 };
 
-// Keeper grouping (blocking.cpp:431-547) on the host, bit-exact.
-void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* cols, float tau,
-                          int64_t col_block, int64_t max_row_block, std::vector<int64_t>& grouping,
-                          int64_t& comparisons, int64_t& merges);
+// Distances of a chunk of Keeper candidates on a device: init() takes every
+// row's block-column runs once; fill() writes, for rows j0 .. j1 - 1, the
+// Jaccard distance (JaccardDistanceGroup, blocking.cpp:904-975) of the
+// row's runs to the given pattern runs at group size g into out[j - j0]
+// (every row, grouped or not: the caller reads the ones it compares).
+struct KeeperDevice {
+  virtual ~KeeperDevice() {}
+  virtual bool init(const std::vector<int64_t>& runs, const std::vector<int64_t>& run_ptr) = 0;
+  virtual bool fill(const int64_t* pattern, int64_t np, int64_t g, int64_t j0, int64_t j1, float* out) = 0;
+  virtual const char* error() const = 0;
+};
+// A KeeperDevice on CUDA device `device` (reorder_gpu.cu); nullptr if the
+// device cannot be used.
+KeeperDevice* make_keeper_device(int device);
+
+// Keeper grouping (blocking.cpp:431-547), bit-exact: the seed loop on the
+// host; candidate distances on the host's cores, or on `dev` when given.
+// Returns false when the device failed (its error() says why).
+bool keeper_grouping(int64_t rows, const int64_t* rowptr, const int32_t* cols, float tau, int64_t col_block,
+                     int64_t max_row_block, std::vector<int64_t>& grouping, int64_t& comparisons, int64_t& merges,
+                     KeeperDevice* dev);
+inline void keeper_grouping_host(int64_t rows, const int64_t* rowptr, const int32_t* cols, float tau,
+                                 int64_t col_block, int64_t max_row_block, std::vector<int64_t>& grouping,
+                                 int64_t& comparisons, int64_t& merges) {
+  keeper_grouping(rows, rowptr, cols, tau, col_block, max_row_block, grouping, comparisons, merges, nullptr);
+}
 // get_permutation / get_fixed_size_grouping (utilities.cpp:8-20, 45-54).
 std::vector<int64_t> permutation_of(const std::vector<int64_t>& grouping);
 std::vector<int64_t> fixed_size_grouping(const std::vector<int64_t>& grouping, int64_t row_block);

@@ -139,8 +139,8 @@ class ReorderResult:
 def reorder(csr: Csr, tau: float = 0.5, col_block: int = 16, row_block: int = 16, algo: int = 5,
             force_fixed: bool = True, use_gpu: bool = False) -> ReorderResult:
     """Row reordering with the reference's result: new row r = old row perm[r].
-    The scan runs on the host's cores; use_gpu=True is rejected
-    (SMAT_ERR_UNSUPPORTED)."""
+    use_gpu=True measures the candidate distances on the current CUDA device
+    (the seed loop and its commits stay on the host); same result."""
     perm = np.zeros(csr.rows, np.int64)
     grouping = np.zeros(csr.rows, np.int64)
     st = ReorderStats()
