@@ -9,10 +9,14 @@ matrices) for the shape in one forward pass. The sweep stays the fallback and
 the judge: regret = t(predicted) / t(sweep best) - 1. The tensor-core SpMM
 needs 16-column blocks, so the 8x8 shape is never available (never a label).
 
-    python -m smat.selector --out DIR [--train 160] [--test 40] [--seed 1]
+    python -m smat.selector --out DIR [--train 600] [--test 200] [--seed 1]
+                            [--rows-min 8192] [--rows-max 32768]
 
 builds the dataset (sweeps), trains, and writes DIR/selector_sweep.npz,
-DIR/selector_weights.npz and a JSON summary line with the regrets.
+DIR/selector_weights.npz and a JSON summary line with the regrets. The
+reorders of the sweep run in a pool of single-threaded worker processes,
+one matrix per job (each regenerates its matrix from its seed), while the
+parent times the SpMMs of the matrices already reordered on the GPU.
 """
 from __future__ import annotations
 
@@ -42,11 +46,34 @@ def family_matrix(family: int, rows: int, rng: np.random.Generator):
         scale = max(8, int(np.ceil(np.log2(rows))))
         A = G.rmat(scale, int(rng.integers(4, 48)) * (1 << scale), seed=seed)
     elif family == 2:
-        A = G.random_block(rows, float(rng.uniform(0.005, 0.05)), float(rng.uniform(0.2, 0.9)), 0.95, seed=seed)
+        # block density 0.5-2 %, fill 20-95 %: at most ~2 % of the entries, as the sweep's families are stated
+        A = G.random_block(rows, float(rng.uniform(0.005, 0.02)), float(rng.uniform(0.2, 0.9)), 0.95, seed=seed)
     else:
         A = G.stencil27(max(8, int(round(rows ** (1 / 3)))), seed=seed)
     perm = rng.permutation(A.rows)                 # scrambled rows: the reordering has work to do
     return A.permuted(perm)
+
+
+def spec_matrix(spec):
+    """The matrix of a dataset entry (family, rows, seed), regenerated deterministically."""
+    family, rows, mseed = spec
+    return family_matrix(int(family), int(rows), np.random.default_rng(int(mseed)))
+
+
+def _sweep_job(job):
+    """(index, {(t, b): perm}) for one matrix: every tau and supported block
+    shape, in a worker process (CPU only, one thread)."""
+    i, spec = job
+    from . import reorder
+    A = spec_matrix(spec)
+    out = {}
+    for t, tau in enumerate(TAUS):
+        for b, (bh, bw) in enumerate(BLOCKS):
+            if bw != 16:
+                continue
+            out[(t, b)] = reorder(A, tau=tau, col_block=bw, row_block=bh, algo=5,
+                                  force_fixed=True).perm.astype(np.int32)
+    return i, out
 
 
 def _reorder_job(args):
@@ -96,24 +123,49 @@ def time_spmm(A, perm, block, device=0, reps=10):
     return e0.elapsed_time(e1) / reps
 
 
-def build_dataset(n: int, seed: int, rows_range=(2048, 8192), device=0, log=print):
-    """Features [n, 64] and sweep times [n, 9, 3] (inf where a shape is unavailable)."""
-    from . import features
+def dataset_specs(n: int, seed: int, rows_range=(8192, 32768)):
+    """(family, rows, matrix seed) per entry: families in turn, rows log-uniform."""
     rng = np.random.default_rng(seed)
-    mats = []
+    specs = []
     for i in range(n):
         rows = int(np.exp(rng.uniform(np.log(rows_range[0]), np.log(rows_range[1]))))
-        mats.append(family_matrix(i % 4, rows, rng))
-    t0 = time.time()
-    perms = sweep_perms(mats)
-    log(f"[selector] {len(perms)} reorders in {time.time() - t0:.1f}s")
-    X = np.stack([features(A, device) for A in mats])
+        specs.append((i % 4, rows, int(rng.integers(1 << 62))))
+    return np.array(specs, np.int64)
+
+
+def build_dataset(n: int, seed: int, rows_range=(8192, 32768), device=0, log=print, workers=None):
+    """(specs [n, 3], features [n, 64], sweep times [n, 9, 3]; inf where a
+    shape is unavailable). Largest matrices are reordered first."""
+    import multiprocessing as mp
+
+    from . import features
+    specs = dataset_specs(n, seed, rows_range)
+    X = np.zeros((n, 64), np.float32)
     T = np.full((n, len(TAUS), len(BLOCKS)), np.inf)
+    order = sorted(range(n), key=lambda i: -int(specs[i][1]))
+    jobs = [(i, tuple(specs[i])) for i in order]
     t0 = time.time()
-    for (m, t, b), perm in perms.items():
-        T[m, t, b] = time_spmm(mats[m], perm, BLOCKS[b], device)
-    log(f"[selector] {len(perms)} SpMM timings in {time.time() - t0:.1f}s")
-    return X.astype(np.float32), T
+    nproc = workers or max(1, (os.cpu_count() or 2) - 1)
+    old = os.environ.get("OMP_NUM_THREADS")
+    os.environ["OMP_NUM_THREADS"] = "1"           # one core per worker process
+    try:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(nproc) as pool:
+            done = 0
+            for i, perms in pool.imap_unordered(_sweep_job, jobs):
+                A = spec_matrix(specs[i])
+                X[i] = features(A, device)
+                for (t, b), perm in perms.items():
+                    T[i, t, b] = time_spmm(A, perm.astype(np.int64), BLOCKS[b], device)
+                done += 1
+                if done % 50 == 0 or done == n:
+                    log(f"[selector] {done}/{n} matrices swept, {time.time() - t0:.0f}s")
+    finally:
+        if old is None:
+            os.environ.pop("OMP_NUM_THREADS", None)
+        else:
+            os.environ["OMP_NUM_THREADS"] = old
+    return specs, X, T
 
 
 def labels(T):
@@ -213,16 +265,21 @@ def regret(T, ti, bi):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
-    ap.add_argument("--train", type=int, default=160)
-    ap.add_argument("--test", type=int, default=40)
+    ap.add_argument("--train", type=int, default=600)
+    ap.add_argument("--test", type=int, default=200)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--epochs", type=int, default=400)
+    ap.add_argument("--rows-min", type=int, default=8192)
+    ap.add_argument("--rows-max", type=int, default=32768)
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     n = args.train + args.test
-    X, T = build_dataset(n, args.seed)
-    np.savez_compressed(os.path.join(args.out, "selector_sweep.npz"), X=X, T=T, taus=np.array(TAUS),
-                        blocks=np.array(BLOCKS), train=np.array(args.train))
+    t0 = time.time()
+    specs, X, T = build_dataset(n, args.seed, (args.rows_min, args.rows_max))
+    sweep_s = time.time() - t0
+    np.savez_compressed(os.path.join(args.out, "selector_sweep.npz"), X=X, T=T, specs=specs, taus=np.array(TAUS),
+                        blocks=np.array(BLOCKS), train=np.array(args.train),
+                        rows_range=np.array([args.rows_min, args.rows_max]))
     yt, yb = labels(T)
     sel = Selector(seed=args.seed)
     hist = sel.train(X[:args.train], yt[:args.train], yb[:args.train], epochs=args.epochs)
@@ -231,7 +288,8 @@ def main():
     r = regret(Tt, ti, bi)
     r0 = regret(Tt, np.full(len(Tt), DEFAULT[0]), np.full(len(Tt), DEFAULT[1]))
     np.savez_compressed(os.path.join(args.out, "selector_weights.npz"), params=sel.params())
-    print(json.dumps({"train": args.train, "test": args.test, "final_loss": hist[-1], "first_loss": hist[0],
+    print(json.dumps({"train": args.train, "test": args.test, "rows": [args.rows_min, args.rows_max],
+                      "sweep_seconds": sweep_s, "final_loss": hist[-1], "first_loss": hist[0],
                       "regret_mean": float(r.mean()), "regret_p90": float(np.quantile(r, 0.9)),
                       "regret_default_mean": float(r0.mean()), "regret_default_p90": float(np.quantile(r0, 0.9)),
                       "best_is_default_frac": float(np.mean(r0 == 0))}), flush=True)
