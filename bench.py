@@ -140,35 +140,6 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def l2_read_gbs(dev, mb=64, reps=50):
-    """Read bandwidth from L2 on this GPU, measured here: a sum over an
-    L2-resident FP16 buffer (mb MiB, well inside the 129 MB L2), replayed
-    from a CUDA graph. A proxy for the rate at which SMs can pull tiles out
-    of L2 (the SpMM's B tiles and A stages all pass through it)."""
-    import torch
-    x = torch.ones(mb * (1 << 20) // 2, dtype=torch.float16, device=dev)
-    out = torch.empty((), dtype=torch.float32, device=dev)
-    s = torch.cuda.Stream(device=dev)
-    with torch.cuda.stream(s):
-        for _ in range(3):
-            torch.sum(x, dim=0, dtype=torch.float32, out=out)
-    torch.cuda.synchronize(dev)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g, stream=s):
-        for _ in range(reps):
-            torch.sum(x, dim=0, dtype=torch.float32, out=out)
-    with torch.cuda.stream(s):
-        g.replay()
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    with torch.cuda.stream(s):
-        g.replay()
-    e1.record(s)
-    torch.cuda.synchronize(dev)
-    return x.numel() * 2 * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
-
-
 def profile_traffic():
     """DRAM bytes per launch of the SpMM kernel from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "spmm_tc_rmat16_traffic.json")
@@ -477,7 +448,6 @@ def run_smat(args):
     # (blocks + MMA list) and one 4 KB B tile per distinct block column of a
     # panel (n_union_cols per 128-column pass)
     staged = nnzb * 512 + info["n_union_cols"] * 4096 * ((N + 127) // 128)
-    l2_gbs = l2_read_gbs(dev)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -493,12 +463,12 @@ def run_smat(args):
                      "traffic_source": (tr["source"] if tr else None),
                      "algorithmic_bytes_per_launch": alg_bytes, "kernel": "spmm_tc_kernel",
                      "kernel_ms": kern_ms, "pack_b_ms": pack_ms},
-        "staging_roofline": {"bound": "l2", "bytes_per_launch": staged,
-                             "achieved": staged / (kern_ms * 1e-3) / 1e9,
-                             "peak": l2_gbs, "unit": "GB/s", "frac": staged / (kern_ms * 1e-3) / 1e9 / l2_gbs,
-                             "peak_kind": "measured here: sum over an L2-resident 64 MiB buffer",
-                             "note": "A blocks + one 4 KB B tile per distinct block column of a 16-row panel, "
-                                     "the bytes the stages pull through L2 (ncu: 1.86 GB L2->SM per launch)"},
+        "staging": {"bytes_per_launch": staged, "achieved_gbs": staged / (kern_ms * 1e-3) / 1e9,
+                    "bytes_per_clk_per_sm": staged / (kern_ms * 1e-3) / 152 / (clk["sm_mhz"] * 1e6)
+                    if clk.get("sm_mhz") else None,
+                    "note": "what the stages pull from L2 into shared memory: every A block once plus one 4 KB B "
+                            "tile per distinct block column of a 16-row panel (ncu: 1.86 GB L2->SM per launch); "
+                            "the roofline above counts B once"},
         "clocks": clk,
         "e2e": {"value": world * useful / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": A.cols * N * 2, "d2h_bytes_per_step": A.rows * N * 4, "ms_per_step": e2e_ms},
