@@ -22,7 +22,6 @@
 
 #include <algorithm>
 #include <cstdint>
-#include <memory>
 #include <string>
 #include <vector>
 
@@ -97,6 +96,7 @@ class CudaKeeper final : public KeeperDevice {
   bool init(const std::vector<int64_t>& runs, const std::vector<int64_t>& run_ptr) override {
     if (!set_device()) return false;
     if (!ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream")) return false;
+    if (!ok(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_), "SM count")) return false;
     std::vector<int32_t> r32(runs.size());
     for (size_t i = 0; i < runs.size(); i++) {
       if (runs[i] < 0 || runs[i] > INT32_MAX) return bad("block-column id out of 32-bit range");
@@ -143,7 +143,7 @@ class CudaKeeper final : public KeeperDevice {
                       "copy pattern"))
       return false;
     const int threads = 256;
-    const int64_t blocks = std::min<int64_t>((n + threads - 1) / threads, 152 * 8);
+    const int64_t blocks = std::min<int64_t>((n + threads - 1) / threads, (int64_t)sms_ * 8);
     dev::keeper_dist_kernel<<<(unsigned)blocks, threads, 0, stream_>>>(d_runs_, d_ptr_, d_pat_, np, g, j0, j1, d_out_);
     if (!ok(cudaGetLastError(), "distance kernel launch") ||
         !ok(cudaMemcpyAsync(h_out_, d_out_, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, stream_),
@@ -169,6 +169,7 @@ class CudaKeeper final : public KeeperDevice {
   }
 
   int device_;
+  int sms_ = 1;
   int64_t rows_ = 0;
   cudaStream_t stream_ = nullptr;
   int32_t* d_runs_ = nullptr;
