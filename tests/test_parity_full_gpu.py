@@ -6,6 +6,9 @@
   FP16: the plain FP16 form within 1e-3 relative Frobenius error of the FP64
   product, and the uploaded BCSR bit-equal to the host blocking of the
   reordered matrix (csrToBcsr, src/cuda_hgemm/src/common/matrix.h:666-792).
+* The same R-MAT workload with its exact-2:4 blocks on the structured-sparse
+  path (every such block, and only units of at least 8 of them): FP16
+  within 1e-3 of FP64.
 * 27-point stencil on 64^3 (262,144 rows, 6.86 M nonzeros), B 262144 x 256
   FP32 N(0,1): FP16 <= 1e-3, BF16 <= 1e-2, split hi+lo BF16 <= 1e-4 (the
   stated bound is 1e-3) and FP8 e4m3 with per-block scales <= 2e-2, all
@@ -53,6 +56,27 @@ def test_rmat16_workload_plain_fp16(dev, smat_mod, oracle_lib):
     e = rel(Cm.cpu().numpy(), ref)
     print(f"R-MAT 2^16 workload ({A.nnz} nnz, {M.info['nnzb']} blocks): FP16 rel err vs FP64 {e:.3e}")
     assert e <= 1e-3
+    M.close()
+
+
+@pytest.mark.parametrize("unit_min", [1, 8])
+def test_rmat16_workload_with_24_path(dev, smat_mod, oracle_lib, unit_min):
+    from smat import workloads
+    A, perm = workloads.rmat16()
+    M = smat_mod.Bcsr(A, block=(16, 16), forms=(smat_mod.FORM_F16,), row_perm=perm, use_24=unit_min)
+    n24 = M.info["n_blocks_24"]
+    assert n24 > 0
+    N = 128
+    Bh = np.random.default_rng(2).uniform(-1, 1, (A.cols, N)).astype(np.float16)
+    B = torch.from_numpy(Bh).to(dev).t().contiguous().t()
+    Cm = M.spmm(B, form=smat_mod.FORM_F16)
+    torch.cuda.synchronize()
+    M.check_device_error()
+    ref = oracle_lib.spmm_f64(A.row_ptr, A.col_idx, A.values.astype(np.float64), Bh.astype(np.float64))
+    err = rel(Cm.cpu().numpy(), ref)
+    print(f"R-MAT 2^16 workload, 2:4 path (units of >= {unit_min}): {n24} of {M.info['nnzb']} blocks on mma.sp, "
+          f"rel err vs FP64 {err:.3e}")
+    assert err <= 1e-3, err
     M.close()
 
 
