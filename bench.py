@@ -273,6 +273,104 @@ def run_reorder(args):
     print(json.dumps(line), flush=True)
 
 
+TILES_WORKLOAD = {
+    "workload": "rmat16_reordered_tiles4x4",
+    "source": "the R-MAT workload's reordered BCSR (tau 0.6, 30 % of blocks forced to 2:4)",
+    "step": "smat_tiles_create: device BCSR -> the reference's merged 4 x 4-block tiles (synchronous)",
+    "spmm": "mmaOBTKernel_tiled / mmaOBTSKernel_tiled_large on the merged arrays, N = 128, FP16 B (column-major) "
+            "and C, legacy default stream",
+}
+
+
+def run_tiles(args):
+    """The merged 4 x 4-block tiles of the reference's bcsrBlocking
+    (matrix.h:794-1137) built on the GPU from the R-MAT workload's BCSR, at
+    16 x 16 and 16 x 32 blocks: seconds per build (wall clock: the build
+    synchronises), checked bit for bit against the oracle's host build (also
+    timed, one thread), and the `_tiled` launcher's SpMM on the result
+    (CUDA events) with its error against FP64 on a row sample."""
+    import scipy.sparse as sps
+    import torch
+
+    import smat
+    from smat import _lib
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    dev = torch.device("cuda", 0)
+    A, perm = build_matrix()
+    N = 128
+    rng = np.random.default_rng(2)
+    for k in (16, 32):
+        brp, bci, bv = smat.csr_to_bcsr_host(A, block=(16, k), row_perm=perm)
+        M, K = (A.rows + 15) // 16 * 16, (A.cols + k - 1) // k * k
+        up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        drp, dci, dv = up(brp), up(bci), up(bv.reshape(-1).view(np.int16))
+        torch.cuda.synchronize()
+        times, T = [], None
+        for i in range(args.warmup + args.steps):
+            if T is not None:
+                T.close()
+            t0 = time.perf_counter()
+            T = smat.Tiles(M, K, k, drp, dci, dv)
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                times.append(dt)
+        got = T.to_host()
+        t0 = time.perf_counter()
+        want = O.bcsr_blocking(M, K, k, brp, bci, bv)
+        t_host = time.perf_counter() - t0
+        exact = all(np.array_equal(got[x].reshape(-1), want[x].reshape(-1)) for x in O.TILE_KEYS)
+        del want
+        # the _tiled launcher on the merged arrays (C rows in the reordered order)
+        Bh = np.zeros((K, N), np.float16)
+        Bh[: A.cols] = rng.uniform(-1, 1, (A.cols, N)).astype(np.float16)
+        Bc = torch.from_numpy(Bh).to(dev).t().contiguous()
+        Cm = torch.empty((M, N), dtype=torch.float16, device=dev)
+        d = T.desc
+        name = "mmaOBTKernel_tiled" if k == 16 else "mmaOBTSKernel_tiled_large"
+        f = _lib.ref_shim(name)
+
+        def call():
+            if k == 16:
+                f(d.values, d.row_ptr, d.col_idx, Bc.data_ptr(), Cm.data_ptr(), M, N, K, len(bci), d.block_info,
+                  d.rel_map)
+            else:
+                f(d.values, d.row_ptr, d.col_idx, None, None, Bc.data_ptr(), Cm.data_ptr(), M, N, K, len(bci),
+                  d.block_info, d.rel_map, d.tile_info)
+
+        for _ in range(max(args.warmup, 1)):
+            call()
+        torch.cuda.synchronize()
+        st = smat.lib().smat_ref_shims_last_status()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / max(args.steps, 1)
+        rows = np.sort(rng.choice(A.rows, min(4096, A.rows), replace=False))
+        src = perm[rows]
+        Asp = sps.csr_matrix((A.values.astype(np.float64), A.col_idx, A.row_ptr), shape=(A.rows, A.cols))
+        ref = Asp[src] @ Bh[: A.cols].astype(np.float64)
+        Cs = Cm.float().cpu().numpy()[rows].astype(np.float64)
+        err = float(np.linalg.norm(Cs - ref) / np.linalg.norm(ref))
+        smat.lib().smat_ref_shims_release()
+        print(json.dumps({
+            "metric": "merged-tile build seconds", "value": float(np.median(times)), "unit": "s",
+            "higher_is_better": False, "steps": len(times), "warmup": args.warmup, "data": "synthetic",
+            "config": dict(TILES_WORKLOAD, block=[16, k]), "nnzb": int(len(bci)), "n_tiles": int(T.n_tiles),
+            "n_rowptr": int(T.n_rowptr), "bit_exact_vs_oracle": bool(exact),
+            "cpu_baseline": {"value": t_host, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "whole matrix; the oracle's restatement of bcsrBlocking (map lookup in "
+                                       "place of the reference's linear search over the tiles made so far)"},
+            "tiled_spmm": {"launcher": name, "ms": ms, "status": int(st),
+                           "useful_tflops": 2.0 * A.nnz * N / (ms * 1e-3) / 1e12,
+                           "rel_err_vs_fp64_4096_rows": err},
+        }), flush=True)
+        T.close()
+
+
 def run_smat(args):
     import torch
 
@@ -882,11 +980,12 @@ def main():
     ap.add_argument("--impl", default="smat", choices=["smat", "reference"])
     ap.add_argument("--workload", default="rmat16",
                     choices=["rmat16", "stencil64_forms", "batched512", "rmat16_libraries", "rmat16_reorder",
-                             "pruned24"],
+                             "pruned24", "rmat16_tiles"],
                     help="rmat16: the headline SpMM line; stencil64_forms: one line per precision form; "
                          "batched512: grouped vs sequential SpMMs; rmat16_libraries: cuSPARSE on the "
                          "headline inputs, for comparison; rmat16_reorder: the reorder step alone "
-                         "(with --impl reference: the reference's own reorder)")
+                         "(with --impl reference: the reference's own reorder); rmat16_tiles: the merged "
+                         "4 x 4-block tiles built on the GPU and the _tiled launchers on them")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--no-sp24", action="store_true", help="skip the structured-sparse (2:4) path's line")
     ap.add_argument("--no-tune", action="store_true", help="stencil forms: skip the autotuned lines")
@@ -904,6 +1003,8 @@ def main():
         run_libraries(args)
     elif args.workload == "pruned24":
         run_pruned24(args)
+    elif args.workload == "rmat16_tiles":
+        run_tiles(args)
     else:
         run_smat(args)
 

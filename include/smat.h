@@ -228,6 +228,50 @@ smat_status smat_csr_to_bcsr_split_host(const smat_csr* A, int32_t block_cols, c
                                         uint16_t* values_24, int32_t* row_ptr_dense, int32_t* col_idx_dense,
                                         uint16_t* values_dense, int32_t* block_info);
 
+/* The reference's merged 4 x 4-block tiles (SparseMatrix::bcsrBlocking,
+ * src/cuda_hgemm/src/common/matrix.h:794-1137, whose output feeds the
+ * `_tiled` launchers mmaOBTKernel_tiled / mmaOBTSKernel_tiled_large), built
+ * on the GPU from a DEVICE BCSR as csrToBcsr lays it out: row_ptr[rows/16+1],
+ * col_idx[nnzb] (column starts, ascending in each block row),
+ * values[nnzb*16*block_cols] FP16 bits row-major per block (16-byte
+ * aligned); block_cols 16 or 32; rows a multiple of 16, cols of block_cols.
+ * The result is bit-identical to the reference's merged arrays:
+ *   values     [n_tiles][4][4][16][block_cols] FP16 bits (block-major tiles,
+ *              tiles numbered in order of first appearance in BCSR order)
+ *   row_ptr    [n_rowptr]: one entry per tile row holding a tile, then
+ *              n_tiles (tile rows without a tile get no entry, as there)
+ *   col_idx    [n_tiles]: column start of each tile (a multiple of 4k)
+ *   block_info [tile_rows * tile_cols]: 1 where a tile exists
+ *   rel_map    [tile_rows * tile_cols]: tile rank in grid order, or -1
+ *   tile_info  [n_tiles * 16]: the reference's 0 / 1 / 2 labels, computed as
+ *              it computes them (the tile read as a row-major 64 x 4k matrix)
+ * with tile_rows = ceil(rows/64), tile_cols = ceil(cols/(4*block_cols)).
+ * Runs on `stream` and synchronises it (the tile count sizes the outputs);
+ * allocates its outputs and scratch on the current device. Invalid row
+ * pointers or column starts give SMAT_ERR_INVALID. */
+typedef struct smat_tiles smat_tiles; /* opaque, owns the device arrays */
+typedef struct smat_tiles_desc {
+  int64_t rows, cols;
+  int32_t block_cols;
+  int32_t device;
+  int64_t n_tiles, n_rowptr, tile_rows, tile_cols;
+  const uint16_t* values;     /* (device) */
+  const int32_t* row_ptr;     /* (device) */
+  const int32_t* col_idx;     /* (device) */
+  const int32_t* block_info;  /* (device) */
+  const int32_t* rel_map;     /* (device) */
+  const int32_t* tile_info;   /* (device) */
+} smat_tiles_desc;
+smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t block_cols, int64_t nnzb,
+                              const int32_t* row_ptr, const int32_t* col_idx, const void* values,
+                              void* stream, smat_tiles** out);
+smat_status smat_tiles_describe(const smat_tiles* t, smat_tiles_desc* out);
+/* Host copies of the arrays above (any pointer may be NULL), sized as
+ * described: the reference's mergedBcsr*_host / merged*_host arrays. */
+smat_status smat_tiles_copy_to_host(const smat_tiles* t, int32_t* row_ptr, int32_t* col_idx, uint16_t* values,
+                                    int32_t* block_info, int32_t* rel_map, int32_t* tile_info);
+smat_status smat_tiles_destroy(smat_tiles* t);
+
 /* ---------------------------------------------------------------- step 3 */
 
 /* Bytes of device scratch smat_spmm needs for this form / B dtype / N: the

@@ -47,6 +47,21 @@ void mmaOBTSKernel_large_separate(half* bcsrValuesA_sparse, int* bcsrRowPtrA_spa
                                   half* bcsrValuesA_dense, int* bcsrRowPtrA_dense, int* bcsrColIdxA_dense,
                                   char* metadata, half* sparseMatrixA, half* B, half* C, size_t M, size_t N, size_t K,
                                   size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping);
+/* mmaOBT_tiled.cu:208-217 (HGEMM_FUNC_SPARSE2, main.cu:55): the matrix as
+ * the merged 4 x 4-block tiles of SparseMatrix::bcsrBlocking (matrix.h:
+ * 794-1137; built on the GPU by smat_tiles_create), 16 x 16 blocks:
+ * bcsrValuesA / bcsrRowPtrA / bcsrColIdxA are the merged values, tile row
+ * pointer and tile column starts, blockInfo the merged tile grid
+ * (required: it sizes the arrays); nonzeroBlocks only keys the cache. Each
+ * tile's values are read at its own position in the arrays. */
+void mmaOBTKernel_tiled(half* bcsrValuesA, int* bcsrRowPtrA, int* bcsrColIdxA, half* B, half* C, size_t M, size_t N,
+                        size_t K, size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping);
+/* mmaOBTS_tiled_large.cu:431-451 (HGEMM_FUNC_SPARSE24_2_tiled, main.cu:58):
+ * the same for tiles of 16 x 32 blocks; metadata, sparseMatrixA and
+ * tileInfo are not read (the product comes from the merged values). */
+void mmaOBTSKernel_tiled_large(half* bcsrValuesA, int* bcsrRowPtrA, int* bcsrColIdxA, char* metadata,
+                               half* sparseMatrixA, half* B, half* C, size_t M, size_t N, size_t K,
+                               size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping, int* tileInfo);
 /* mmaST.cu:22-140 launcher (main.cu:60-63): the reference's 2:4 compression
  * of the blocks blockInfo marks 1, into its own metadata / value layout. */
 void preprocessing_mmaSTKernel(half* bcsrValuesA, char* metadata, half* sparseMatrixA, size_t M, size_t N, size_t K,

@@ -59,6 +59,10 @@ def lib():
         L.orc_csr_to_bcsr.restype = C.c_int64
         L.orc_csr_to_bcsr.argtypes = [C.c_int64, C.c_int64, C.c_int, _i32p, _i32p, _u16p,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_bcsr_blocking.restype = C.c_int64
+        L.orc_bcsr_blocking.argtypes = [C.c_int64, C.c_int64, C.c_int, C.c_int64, _i32p, _i32p, _u16p,
+                                        C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]
         L.orc_is_block_24.restype = C.c_int
         L.orc_is_block_24.argtypes = [_u16p, C.c_int, C.c_int]
         L.orc_spmm_f64.restype = None
@@ -123,10 +127,21 @@ class _RefBcsr(C.Structure):
                 ("rel_map", C.POINTER(C.c_int32))]
 
 
+class _RefTiles(C.Structure):
+    _fields_ = [("ntiles", C.c_int64), ("n_rowptr", C.c_int64), ("grid", C.c_int64),
+                ("rowptr", C.POINTER(C.c_int32)), ("colidx", C.POINTER(C.c_int32)),
+                ("val", C.POINTER(C.c_uint16)), ("block_info", C.POINTER(C.c_int32)),
+                ("rel_map", C.POINTER(C.c_int32)), ("tile_info", C.POINTER(C.c_int32))]
+
+
 def ref_bcsr_lib():
     global _ref_bcsr
     if _ref_bcsr is None:
         L = C.CDLL(os.path.join(REFDIR, "libsmat_ref_bcsr.so"))
+        L.ref_bcsr_blocking.restype = C.POINTER(_RefTiles)
+        L.ref_bcsr_blocking.argtypes = [C.c_int64, C.c_int64, C.c_int, C.c_int64, _i32p, _i32p, _u16p]
+        L.ref_tiles_free.restype = None
+        L.ref_tiles_free.argtypes = [C.POINTER(_RefTiles)]
         L.ref_csr_to_bcsr.restype = C.POINTER(_RefBcsr)
         L.ref_csr_to_bcsr.argtypes = [C.c_int64, C.c_int64, C.c_int, C.c_int64, _i32p, _i32p, _u16p]
         L.ref_bcsr_free.restype = None
@@ -235,6 +250,49 @@ def ref_csr_to_bcsr(m_row, m_col, k, rowptr, colidx, val_f16):
     info = np.ctypeslib.as_array(b.block_info, shape=(max(grid, 1),))[:grid].copy()
     L.ref_bcsr_free(p)
     return brp, bci, bv.view(np.float16).reshape(nnzb, 16, k), info
+
+
+TILE_KEYS = ("rowptr", "colidx", "val", "block_info", "rel_map", "tile_info")
+
+
+def bcsr_blocking(m_row, m_col, k, brp, bci, bval_f16):
+    """Oracle of SparseMatrix::bcsrBlocking (matrix.h:794-1137): the 4 x 4-block
+    merged tiles of a BCSR, as a dict of TILE_KEYS (values as FP16 bits,
+    [ntiles, 256 * k])."""
+    brp = np.ascontiguousarray(brp, np.int32)
+    bci = np.ascontiguousarray(bci, np.int32)
+    vb = np.ascontiguousarray(np.asarray(bval_f16, np.float16).view(np.uint16)).reshape(-1)
+    L = lib()
+    nnzb = len(bci)
+    nrp = C.c_int64()
+    nt = L.orc_bcsr_blocking(m_row, m_col, k, nnzb, brp, bci, vb, C.byref(nrp), None, None, None, None, None,
+                             None)
+    grid = ((m_row + 63) // 64) * ((m_col + 4 * k - 1) // (4 * k))
+    out = {"rowptr": np.zeros(nrp.value, np.int32), "colidx": np.zeros(max(nt, 1), np.int32),
+           "val": np.zeros(max(nt, 1) * 256 * k, np.uint16), "block_info": np.zeros(max(grid, 1), np.int32),
+           "rel_map": np.zeros(max(grid, 1), np.int32), "tile_info": np.zeros(max(nt, 1) * 16, np.int32)}
+    L.orc_bcsr_blocking(m_row, m_col, k, nnzb, brp, bci, vb, C.byref(nrp), *(out[n].ctypes.data for n in TILE_KEYS))
+    out["colidx"], out["tile_info"] = out["colidx"][:nt], out["tile_info"][: nt * 16]
+    out["val"] = out["val"][: nt * 256 * k].reshape(nt, 256 * k)
+    out["block_info"], out["rel_map"] = out["block_info"][:grid], out["rel_map"][:grid]
+    return out
+
+
+def ref_bcsr_blocking(m_row, m_col, k, brp, bci, bval_f16):
+    """The reference's own bcsrBlocking, run on the CPU (same dict as bcsr_blocking)."""
+    brp = np.ascontiguousarray(brp, np.int32)
+    bci = np.ascontiguousarray(bci, np.int32)
+    vb = np.ascontiguousarray(np.asarray(bval_f16, np.float16).view(np.uint16)).reshape(-1)
+    L = ref_bcsr_lib()
+    p = L.ref_bcsr_blocking(m_row, m_col, k, len(bci), brp, bci, vb)
+    t = p.contents
+    nt, nrp, grid = t.ntiles, t.n_rowptr, t.grid
+    take = lambda ptr, n: np.ctypeslib.as_array(ptr, shape=(max(n, 1),))[:n].copy()
+    out = {"rowptr": take(t.rowptr, nrp), "colidx": take(t.colidx, nt),
+           "val": take(t.val, nt * 256 * k).reshape(nt, 256 * k), "block_info": take(t.block_info, grid),
+           "rel_map": take(t.rel_map, grid), "tile_info": take(t.tile_info, nt * 16)}
+    L.ref_tiles_free(p)
+    return out
 
 
 def spmm_f64(rowptr, colidx, val, B):

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <set>
 #include <utility>
@@ -268,6 +269,97 @@ int64_t orc_csr_to_bcsr(int64_t m_row, int64_t m_col, int k, const int32_t* rowp
   }
   if (block_info) std::copy(info.begin(), info.end(), block_info);
   return nnzb;
+}
+
+// src/cuda_hgemm/src/common/matrix.h:794-1137 (SparseMatrix::bcsrBlocking):
+// groups the 16 x k blocks of a BCSR (as csrToBcsr builds it) into merged
+// TILES of 4 x 4 blocks (64 rows x 4k columns), restated with a map lookup
+// in place of the reference's linear search over the tiles made so far
+// (the keys are unique, so the result is the same). Reproduced as the
+// reference has it:
+//   * tiles are numbered in order of first appearance while walking the
+//     blocks in BCSR order (:814-902), not sorted by column inside a tile row;
+//   * a tile holds its 16 blocks block-major, each block row-major, at
+//     k*4*(row offset) + 16*(column offset) (:851, :878-879);
+//   * the tile row pointer gets one entry per NON-EMPTY tile row, plus the
+//     final count (:932-958): tile rows without a tile get no entry;
+//   * block_info / rel_map cover the full tile grid, rel_map numbers the
+//     tiles in grid (row-major) order (:921-930);
+//   * tile_info labels each of the 16 positions 0 (all zero) / 1 (no group
+//     of four with more than two nonzeros) / 2, reading the tile's values as
+//     a ROW-MAJOR 64 x 4k matrix (:1036-1088), which is not the layout they
+//     were stored in.
+// Two calls: with out_rowptr NULL it returns the tile count and sets
+// *n_rowptr; the second fills rowptr[*n_rowptr], colidx[ntiles],
+// val[ntiles * 256 * k], block_info / rel_map [tile rows * tile cols] and
+// tile_info[ntiles * 16].
+int64_t orc_bcsr_blocking(int64_t m_row, int64_t m_col, int k, int64_t nnzb, const int32_t* brp,
+                          const int32_t* bci, const uint16_t* bval, int64_t* n_rowptr, int32_t* out_rowptr,
+                          int32_t* out_colidx, uint16_t* out_val, int32_t* block_info, int32_t* rel_map,
+                          int32_t* tile_info) {
+  const int64_t tw = 4 * (int64_t)k, th = 64, tsz = 256 * (int64_t)k;
+  const int64_t ncr = (m_col + tw - 1) / tw, nrr = (m_row + th - 1) / th;
+  std::map<std::pair<int64_t, int64_t>, int64_t> tile_of;
+  std::vector<int64_t> ty, tx;                   // tile row start / column start, by tile
+  std::vector<std::vector<uint16_t>> tv;          // values, by tile
+  int64_t br = 0;
+  for (int64_t i = 0; i < nnzb; i++) {
+    while (br < m_row / 16 && brp[br + 1] <= i) br++;
+    const int64_t row = br * 16, col = bci[i];
+    const int64_t y = row - row % th, x = col - col % tw;
+    auto it = tile_of.find({y, x});
+    int64_t t;
+    if (it == tile_of.end()) {
+      t = (int64_t)ty.size();
+      tile_of[{y, x}] = t;
+      ty.push_back(y);
+      tx.push_back(x);
+      tv.emplace_back(tsz, 0);
+    } else {
+      t = it->second;
+    }
+    const int64_t dst = 4 * (int64_t)k * (row - y) + 16 * (col - x);
+    std::memcpy(tv[t].data() + dst, bval + i * 16 * (int64_t)k, sizeof(uint16_t) * 16 * k);
+  }
+  const int64_t nt = (int64_t)ty.size();
+  std::vector<int32_t> rp;
+  int64_t cur = -1;
+  for (int64_t t = 0; t < nt; t++)
+    if (ty[t] != cur) {
+      cur = ty[t];
+      rp.push_back((int32_t)t);
+    }
+  rp.push_back((int32_t)nt);
+  if (n_rowptr) *n_rowptr = (int64_t)rp.size();
+  if (!out_rowptr) return nt;
+  std::copy(rp.begin(), rp.end(), out_rowptr);
+  std::vector<int32_t> info(nrr * ncr, 0);
+  for (int64_t t = 0; t < nt; t++) {
+    out_colidx[t] = (int32_t)tx[t];
+    std::memcpy(out_val + t * tsz, tv[t].data(), sizeof(uint16_t) * tsz);
+    info[(ty[t] / th) * ncr + tx[t] / tw] = 1;
+  }
+  int32_t r = 0;
+  for (int64_t g = 0; g < nrr * ncr; g++) {
+    block_info[g] = info[g];
+    rel_map[g] = info[g] ? r++ : -1;
+  }
+  for (int64_t t = 0; t < nt; t++)
+    for (int sr = 0; sr < 4; sr++)
+      for (int sc = 0; sc < 4; sc++) {
+        bool any = false, two_four = true;
+        for (int rr = 0; rr < 16; rr++) {
+          const uint16_t* rowp = out_val + t * tsz + (int64_t)(sr * 16 + rr) * tw;
+          for (int g = 0; g < k / 4; g++) {
+            int nz = 0;
+            for (int c = 0; c < 4; c++) nz += (rowp[sc * k + 4 * g + c] & 0x7fff) != 0;
+            if (nz > 0) any = true;
+            if (nz > 2) two_four = false;
+          }
+        }
+        tile_info[t * 16 + sr * 4 + sc] = any ? (two_four ? 1 : 2) : 0;
+      }
+  return nt;
 }
 
 // Exact 2:4 predicate on one bh x bw block (row-major, fp16 bits; +0 and -0

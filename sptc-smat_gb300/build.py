@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", f"-I{INCLUDE}", f"-I{CSRC}"]
 HOSTFLAGS = ["-fPIC", "-fopenmp", "-ffp-contract=off"]
 
-CU_SOURCES = ["api.cu", "spmm_tc.cu", "spmm24.cu", "convert.cu", "spmm_static.cu", "ref_shims.cu", "spmm_24ref.cu", "group.cu", "tune.cu", "features.cu", "mlp.cu", "reorder_gpu.cu"]
+CU_SOURCES = ["api.cu", "spmm_tc.cu", "spmm24.cu", "convert.cu", "spmm_static.cu", "ref_shims.cu", "spmm_24ref.cu", "group.cu", "tune.cu", "features.cu", "mlp.cu", "reorder_gpu.cu", "tiles.cu"]
 CPP_SOURCES = ["reorder.cpp", "bcsr.cpp", "sp24.cpp", "io.cpp"]
 
 

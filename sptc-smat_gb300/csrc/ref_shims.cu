@@ -20,6 +20,9 @@
 // cached handle, allocated on the first call that needs it (the stencil
 // shape, K = 262144 at N = 256, needs 128 MiB).
 //
+// The `_tiled` launchers take the merged 4 x 4-block tiles of bcsrBlocking
+// (see entry_for_tiled) and compute from their values in the same way.
+//
 // The 2:4 variants take the reference's compressed values and metadata, but
 // compute from the uncompressed block values (which hold every block), so the
 // result does not depend on how the reference's blockInfo heuristic labelled
@@ -33,6 +36,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <map>
 #include <mutex>
@@ -259,6 +263,106 @@ void run_separate(const half* vs, const int* rps, const int* cis, const half* vd
   g_last = st;
 }
 
+// Cache entry for a matrix given as the reference's merged 4 x 4-block tiles
+// (SparseMatrix::bcsrBlocking, matrix.h:794-1137; built here by
+// smat_tiles_create): the tiles are taken apart into their 16 x bw blocks on
+// the host and the blocks holding any nonzero bit become a BCSR handle. The
+// tile grid (the launchers' blockInfo argument, mergedBlockInfo) gives the
+// array sizes and which tile rows the row pointer's entries belong to (it has
+// entries only for tile rows holding a tile). Each tile's values are read at
+// its own position in the arrays, so the product is the one the arrays
+// describe; the reference's kernels read a tile's values at its rank in grid
+// order (rel_map), which is the same place whenever a tile row's tiles were
+// first met in column order and no tile row is empty.
+smat_status entry_for_tiled(const half* vals, const int* rowptr, const int* colidx, const int* grid, size_t M,
+                            size_t K, size_t nnzb, int bw, Entry** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return smat::fail(SMAT_ERR_CUDA, "cudaGetDevice failed");
+  if (!grid) return smat::fail(SMAT_ERR_INVALID, "the tiled launchers need the merged tile grid (blockInfo)");
+  if (M % 16 || K % bw) return smat::fail(SMAT_ERR_INVALID, "M and K must be multiples of the block shape");
+  // the block width's bit 8 keeps these entries apart from plain BCSRs at the same addresses
+  const Key key = make_key(dev, M, K, nnzb, bw | 0x100, {vals, rowptr, colidx, grid});
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto it = g_cache.find(key);
+  if (it != g_cache.end()) {
+    *out = &it->second;
+    return SMAT_OK;
+  }
+  const size_t tw = 4 * (size_t)bw, tsz = 256 * (size_t)bw, nbr = M / 16;
+  const size_t nrr = (M + 63) / 64, ncr = (K + tw - 1) / tw;
+  std::vector<int32_t> g(nrr * ncr);
+  if (!g.empty() && cudaMemcpy(g.data(), grid, g.size() * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return smat::fail(SMAT_ERR_CUDA, "copying the tile grid failed");
+  std::vector<size_t> used;  // tile rows holding a tile, ascending
+  size_t nt = 0;
+  for (size_t y = 0; y < nrr; y++) {
+    size_t n = 0;
+    for (size_t x = 0; x < ncr; x++) n += g[y * ncr + x] != 0;
+    if (n) used.push_back(y);
+    nt += n;
+  }
+  std::vector<int32_t> rp(used.size() + 1), ci(nt);
+  std::vector<uint16_t> v(nt * tsz);
+  if (cudaMemcpy(rp.data(), rowptr, rp.size() * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      (nt && cudaMemcpy(ci.data(), colidx, ci.size() * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) ||
+      (nt && cudaMemcpy(v.data(), vals, v.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost) != cudaSuccess))
+    return smat::fail(SMAT_ERR_CUDA, "copying the merged tile arrays to the host failed");
+  if (rp[0] != 0 || (size_t)rp.back() != nt)
+    return smat::fail(SMAT_ERR_INVALID, "merged tile row pointer does not match the tile grid");
+  std::vector<std::vector<std::pair<int32_t, size_t>>> rows(nbr);  // per block row: (column, source offset)
+  for (size_t j = 0; j < used.size(); j++) {
+    if (rp[j] > rp[j + 1]) return smat::fail(SMAT_ERR_INVALID, "merged tile row pointer decreases");
+    for (int32_t t = rp[j]; t < rp[j + 1]; t++) {
+      const int64_t x0 = ci[t];
+      if (x0 < 0 || x0 % (int64_t)tw || (size_t)(x0 / tw) >= ncr || !g[used[j] * ncr + (size_t)(x0 / tw)])
+        return smat::fail(SMAT_ERR_INVALID, "a merged tile's column is not in the tile grid");
+      for (size_t by = 0; by < 4; by++)
+        for (size_t bx = 0; bx < 4; bx++) {
+          const size_t off = (size_t)t * tsz + 16 * (size_t)bw * (4 * by + bx);
+          bool any = false;
+          for (size_t e = 0; e < 16 * (size_t)bw && !any; e++) any = v[off + e] != 0;
+          if (!any) continue;
+          const size_t br = 4 * used[j] + by;
+          if (br >= nbr || (size_t)x0 + bx * bw >= K)
+            return smat::fail(SMAT_ERR_INVALID, "a merged tile holds values outside the matrix");
+          rows[br].push_back({(int32_t)(x0 + bx * bw), off});
+        }
+    }
+  }
+  std::vector<int32_t> brp(nbr + 1, 0), bci;
+  std::vector<uint16_t> bv;
+  for (size_t r = 0; r < nbr; r++) {
+    std::sort(rows[r].begin(), rows[r].end());
+    for (const auto& b : rows[r]) {
+      bci.push_back(b.first);
+      bv.insert(bv.end(), v.begin() + b.second, v.begin() + b.second + 16 * (size_t)bw);
+    }
+    brp[r + 1] = (int32_t)bci.size();
+  }
+  smat_bcsr_opts o{};
+  o.device = dev;
+  smat_bcsr* h = nullptr;
+  smat_status st = smat_bcsr_create_from_bcsr((int64_t)M, (int64_t)K, 16, bw, (int64_t)bci.size(), brp.data(),
+                                              bci.data(), bv.data(), &o, &h);
+  if (st != SMAT_OK) return st;
+  Entry& e = g_cache[key];
+  e.h = h;
+  *out = &e;
+  return SMAT_OK;
+}
+
+void run_tiled(const half* vals, const int* rowptr, const int* colidx, const int* grid, const half* B, half* C,
+               size_t M, size_t N, size_t K, size_t nnzb, int bw) {
+  Entry* e = nullptr;
+  smat_status st = entry_for_tiled(vals, rowptr, colidx, grid, M, K, nnzb, bw, &e);
+  if (st == SMAT_OK) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    st = spmm_entry(*e, B, C, N, K);
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  g_last = st;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
@@ -306,6 +410,22 @@ void mmaOBTSKernel_large_separate(half* bcsrValuesA_sparse, int* bcsrRowPtrA_spa
   (void)blockInfo;
   run_separate(bcsrValuesA_sparse, bcsrRowPtrA_sparse, bcsrColIdxA_sparse, bcsrValuesA_dense, bcsrRowPtrA_dense,
                bcsrColIdxA_dense, B, C, M, N, K, nonzeroBlocks, relativeBlockIndexMapping, 32);
+}
+
+void mmaOBTKernel_tiled(half* bcsrValuesA, int* bcsrRowPtrA, int* bcsrColIdxA, half* B, half* C, size_t M, size_t N,
+                        size_t K, size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping) {
+  (void)relativeBlockIndexMapping;
+  run_tiled(bcsrValuesA, bcsrRowPtrA, bcsrColIdxA, blockInfo, B, C, M, N, K, nonzeroBlocks, 16);
+}
+
+void mmaOBTSKernel_tiled_large(half* bcsrValuesA, int* bcsrRowPtrA, int* bcsrColIdxA, char* metadata,
+                               half* sparseMatrixA, half* B, half* C, size_t M, size_t N, size_t K,
+                               size_t nonzeroBlocks, int* blockInfo, int* relativeBlockIndexMapping, int* tileInfo) {
+  (void)metadata;
+  (void)sparseMatrixA;
+  (void)relativeBlockIndexMapping;
+  (void)tileInfo;
+  run_tiled(bcsrValuesA, bcsrRowPtrA, bcsrColIdxA, blockInfo, B, C, M, N, K, nonzeroBlocks, 32);
 }
 
 // ---------------------------------------------------------------- C helpers

@@ -22,10 +22,10 @@ from dataclasses import dataclass
 import numpy as np
 
 from ._lib import (BF16, COL_MAJOR, E4M3, F16, F32, F64, FORM_BF16, FORM_F16, FORM_FP8, FORM_SPLIT_BF16,
-                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrFile, CsrStruct, Problem, ReorderStats, SmatError, TuneResult,
-                   check, lib, ptr)
+                   ROW_MAJOR, BcsrInfo, BcsrOpts, CsrFile, CsrStruct, Problem, ReorderStats, SmatError, TilesDesc,
+                   TuneResult, check, lib, ptr)
 
-__all__ = ["Csr", "Bcsr", "Group", "autotune", "features", "transpose", "reorder_columns", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
+__all__ = ["Csr", "Bcsr", "Group", "Tiles", "autotune", "features", "transpose", "reorder_columns", "reorder", "read_mtx", "read_el", "write_el", "csr_to_bcsr_host", "partition_rows", "row_slice", "ReorderResult", "SmatError", "lib", "FORM_F16", "FORM_BF16",
            "FORM_FP8", "FORM_SPLIT_BF16", "F32", "F16", "BF16", "F64", "E4M3", "ROW_MAJOR", "COL_MAJOR"]
 
 _VAL_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float16): F16, np.dtype(np.float64): F64}
@@ -423,6 +423,59 @@ class Group:
     def close(self):
         if getattr(self, "_h", None):
             lib().smat_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+TILE_KEYS = ("rowptr", "colidx", "val", "block_info", "rel_map", "tile_info")
+
+
+class Tiles:
+    """The reference's merged 4 x 4-block tiles (SparseMatrix::bcsrBlocking,
+    src/cuda_hgemm/src/common/matrix.h:794-1137) built on the GPU from a
+    device BCSR (smat_tiles_create): row_ptr, col_idx, values are torch CUDA
+    tensors (int32, int32, FP16 or int16 of nnzb * 16 * block_cols) in the
+    layout csrToBcsr leaves; rows and cols padded to the block shape."""
+
+    def __init__(self, rows: int, cols: int, block_cols: int, row_ptr, col_idx, values, stream=0):
+        h = C.c_void_p()
+        check(lib().smat_tiles_create(int(rows), int(cols), int(block_cols), int(col_idx.numel()),
+                                      row_ptr.data_ptr(), col_idx.data_ptr(), values.data_ptr(), stream,
+                                      C.byref(h)))
+        self._h = h
+        d = TilesDesc()
+        check(lib().smat_tiles_describe(h, C.byref(d)))
+        self.desc = d
+        self.n_tiles, self.n_rowptr = d.n_tiles, d.n_rowptr
+        self.grid = (d.tile_rows, d.tile_cols)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def to_host(self) -> dict:
+        """The merged arrays on the host, keyed by TILE_KEYS (values as FP16
+        bits, [n_tiles, 256 * block_cols])."""
+        d, nt = self.desc, self.n_tiles
+        cells = d.tile_rows * d.tile_cols
+        out = {"rowptr": np.zeros(self.n_rowptr, np.int32), "colidx": np.zeros(max(nt, 1), np.int32),
+               "val": np.zeros(max(nt, 1) * 256 * d.block_cols, np.uint16),
+               "block_info": np.zeros(max(cells, 1), np.int32), "rel_map": np.zeros(max(cells, 1), np.int32),
+               "tile_info": np.zeros(max(nt, 1) * 16, np.int32)}
+        check(lib().smat_tiles_copy_to_host(self._h, *(out[k].ctypes.data for k in TILE_KEYS)))
+        out["colidx"], out["tile_info"] = out["colidx"][:nt], out["tile_info"][: nt * 16]
+        out["val"] = out["val"][: nt * 256 * d.block_cols].reshape(nt, 256 * d.block_cols)
+        out["block_info"], out["rel_map"] = out["block_info"][:cells], out["rel_map"][:cells]
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().smat_tiles_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -60,6 +60,14 @@ class BcsrInfo(C.Structure):
                 ("fill", C.c_double), ("n_tile_cols", C.c_int32), ("pipeline_depth", C.c_int32)]
 
 
+class TilesDesc(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("block_cols", C.c_int32), ("device", C.c_int32),
+                ("n_tiles", C.c_int64), ("n_rowptr", C.c_int64), ("tile_rows", C.c_int64),
+                ("tile_cols", C.c_int64), ("values", C.c_void_p), ("row_ptr", C.c_void_p),
+                ("col_idx", C.c_void_p), ("block_info", C.c_void_p), ("rel_map", C.c_void_p),
+                ("tile_info", C.c_void_p)]
+
+
 class ReorderStats(C.Structure):
     _fields_ = [("comparisons", C.c_int64), ("merges", C.c_int64)]
 
@@ -84,6 +92,12 @@ _SIGS = {
     "smat_csr_to_bcsr_split_host": (C.c_int, [C.POINTER(CsrStruct), C.c_int32, C.c_void_p, C.POINTER(C.c_int64),
                                               C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smat_tiles_create": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.POINTER(C.c_void_p)]),
+    "smat_tiles_describe": (C.c_int, [C.c_void_p, C.POINTER(TilesDesc)]),
+    "smat_tiles_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
+    "smat_tiles_destroy": (C.c_int, [C.c_void_p]),
     "smat_spmm_workspace_size": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
     "smat_spmm": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
                             C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_size_t, C.c_void_p]),
@@ -175,6 +189,10 @@ REF_SHIMS = {
     "mmaOBTSKernel_large_separate": ("_Z28mmaOBTSKernel_large_separateP6__halfPiS1_S0_S1_S1_PcS0_S0_S0_mmmmS1_S1_",
                                      [_HP, _IP, _IP, _HP, _IP, _IP, C.c_void_p, _HP, _HP, _HP, _SZ, _SZ, _SZ, _SZ,
                                       _IP, _IP]),
+    "mmaOBTKernel_tiled": ("_Z18mmaOBTKernel_tiledP6__halfPiS1_S0_S0_mmmmS1_S1_",
+                           [_HP, _IP, _IP, _HP, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
+    "mmaOBTSKernel_tiled_large": ("_Z25mmaOBTSKernel_tiled_largeP6__halfPiS1_PcS0_S0_S0_mmmmS1_S1_S1_",
+                                  [_HP, _IP, _IP, C.c_void_p, _HP, _HP, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP, _IP]),
     "preprocessing_mmaSTKernel": ("_Z25preprocessing_mmaSTKernelP6__halfPcS0_mmmmPiS2_",
                                   [_HP, C.c_void_p, _HP, _SZ, _SZ, _SZ, _SZ, _IP, _IP]),
     "preprocessing_mmaSTKernel_large": ("_Z31preprocessing_mmaSTKernel_largeP6__halfPcS0_mmmmPiS2_",

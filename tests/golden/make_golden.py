@@ -13,11 +13,15 @@ own code (built from its sources by oracle/Makefile into oracle/_ref/):
 * golden_io.npz — mmio_allinone (src/cuda_hgemm/src/common/mmio_highlevel.h)
   on seeded MatrixMarket files (general, symmetric, pattern, integer,
   hermitian complex, FP16 rounding edge values) and CSR::read_from_edgelist
-  on seeded edge lists, with the file texts.
+  on seeded edge lists, with the file texts;
+* golden_tiles.npz — SparseMatrix::bcsrBlocking (matrix.h:794-1137), the
+  merged 4 x 4-block tiles, on the csrToBcsr output of seeded CSRs (16 x 16
+  and 16 x 32 blocks, empty tile rows, explicit zeros, 2:4-patterned rows,
+  an empty matrix).
 
 Run it where the reference sources are present:
 
-    python tests/golden/make_golden.py [--reference /path/to/sptc-smat]
+    python tests/golden/make_golden.py [--reference /path/to/sptc-smat] [--only tiles]
 """
 from __future__ import annotations
 
@@ -68,6 +72,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("SMAT_REFERENCE"),
                     help="reference source tree (default: $SMAT_REFERENCE, else the oracle recipe's default)")
+    ap.add_argument("--only", choices=["tiles"], help="write only this fixture file")
     args = ap.parse_args()
     import oracle as O
     if args.reference:
@@ -75,6 +80,9 @@ def main():
     O.build(ref=True)
     if not O.ref_available():
         raise SystemExit("reference build not available")
+    if args.only == "tiles":
+        make_tiles(O)
+        return
     rng = np.random.default_rng(20261203)
     out = {}
 
@@ -231,7 +239,67 @@ def main():
         out[f"el{i}_shape"] = np.array([rows, cols], np.int64)
         out[f"el{i}_rowptr"], out[f"el{i}_colidx"], out[f"el{i}_vals"] = rp, ci, v
     np.savez_compressed(os.path.join(HERE, "golden_io.npz"), **out)
+    make_tiles(O)
     print("golden fixtures written to", HERE)
+
+
+def tile_cases(rng):
+    """(m_row, m_col, k, rowptr, cols, values fp16) CSRs for the merged-tile fixtures."""
+    cases = []
+    for i in range(12):
+        k = 16 if i % 2 == 0 else 32
+        mr = 16 * int(rng.integers(1, 30))
+        mc = k * int(rng.integers(1, 24))
+        rp, cs = rand_pattern(rng, mr, mc, int(rng.integers(1, 50)), shuffle=True)
+        v = rng.standard_normal(len(cs)).astype(np.float16)
+        if i % 3 == 1:                      # explicit zeros
+            v[rng.random(len(v)) < 0.4] = 0
+        if i % 4 == 2:                      # whole tile rows without entries
+            keep = np.ones(len(cs), bool)
+            for r in range(mr):
+                if (r // 64) % 2 == 1:
+                    keep[rp[r]:rp[r + 1]] = False
+            counts = np.array([keep[rp[r]:rp[r + 1]].sum() for r in range(mr)])
+            rp = np.concatenate([[0], np.cumsum(counts)])
+            cs, v = cs[keep], v[keep]
+        cases.append((mr, mc, k, rp, cs, v))
+    # rows with exactly two entries in every group of four columns (2:4 labels)
+    mr, mc, k = 128, 256, 16
+    rp, cs = [0], []
+    for r in range(mr):
+        c = []
+        for g4 in range(0, mc, 4):
+            if rng.random() < 0.3:
+                c += sorted(rng.choice(4, 2, replace=False) + g4)
+        cs += c
+        rp.append(len(cs))
+    cases.append((mr, mc, k, np.array(rp), np.array(cs), rng.standard_normal(len(cs)).astype(np.float16)))
+    cases.append((64, 64, 16, np.zeros(65, np.int64), np.zeros(0, np.int64), np.zeros(0, np.float16)))
+    # tiles first met out of column order inside a tile row (later block rows
+    # reach further left), so the merged column array is not sorted there
+    entries = {0: [200], 16: [5, 130], 40: [100, 255], 70: [250], 80: [10, 70], 127: [3]}
+    rp, cs = [0], []
+    for r in range(128):
+        cs += entries.get(r, [])
+        rp.append(len(cs))
+    cases.append((128, 256, 16, np.array(rp), np.array(cs), np.linspace(-2, 2, len(cs)).astype(np.float16)))
+    return cases
+
+
+def make_tiles(O):
+    rng = np.random.default_rng(20261204)
+    out = {}
+    cases = tile_cases(rng)
+    out["tiles_n"] = np.array(len(cases))
+    for i, (mr, mc, k, rp, cs, v) in enumerate(cases):
+        brp, bci, bv, _ = O.ref_csr_to_bcsr(mr, mc, k, rp.astype(np.int32), cs.astype(np.int32), v)
+        t = O.ref_bcsr_blocking(mr, mc, k, brp, bci, bv)
+        out[f"tiles{i}_dims"] = np.array([mr, mc, k], np.int64)
+        out[f"tiles{i}_brp"], out[f"tiles{i}_bci"] = brp, bci
+        out[f"tiles{i}_bval"] = bv.reshape(-1).view(np.uint16)
+        for key in O.TILE_KEYS:
+            out[f"tiles{i}_{key}"] = t[key]
+    np.savez_compressed(os.path.join(HERE, "golden_tiles.npz"), **out)
 
 
 if __name__ == "__main__":

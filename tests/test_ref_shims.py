@@ -27,6 +27,10 @@ EXPECTED = {
     "unsigned long, unsigned long, int*, int*)",
     "mmaOBTSKernel_large_separate(__half*, int*, int*, __half*, int*, int*, char*, __half*, __half*, __half*, "
     "unsigned long, unsigned long, unsigned long, unsigned long, int*, int*)",
+    "mmaOBTKernel_tiled(__half*, int*, int*, __half*, __half*, unsigned long, unsigned long, unsigned long, "
+    "unsigned long, int*, int*)",
+    "mmaOBTSKernel_tiled_large(__half*, int*, int*, char*, __half*, __half*, __half*, unsigned long, "
+    "unsigned long, unsigned long, unsigned long, int*, int*, int*)",
     "preprocessing_mmaSTKernel(__half*, char*, __half*, unsigned long, unsigned long, unsigned long, "
     "unsigned long, int*, int*)",
     "preprocessing_mmaSTKernel_large(__half*, char*, __half*, unsigned long, unsigned long, unsigned long, "
