@@ -10,10 +10,11 @@
 //   2. tile numbers = exclusive scan of the "maker" flags;
 //   3. makers write their tile's column start, tile row and grid cell; every
 //      block copies its values into its tile (one warp per block, 16-byte
-//      vectors);
+//      vectors) and, from the values in its registers, ORs its share of the
+//      tile's position labels in (warp ballots, one atomic per position);
 //   4. tile-row starts and their ranks (scan) give the tile row pointer; a
-//      scan over the tile grid gives the relative index map; each of the
-//      16 positions of every tile gets its label.
+//      scan over the tile grid gives the relative index map; the label
+//      flags become labels.
 // Scans are a three-launch exclusive scan (chunk sums, one CTA over the sums,
 // chunk scans). The build reads the tile and row counts back twice, so it
 // synchronises the stream it runs on; it allocates its outputs and scratch
@@ -134,24 +135,26 @@ __global__ void tiles_check_rows(Geom g, const int32_t* rowptr, int32_t* bad) {
 }
 
 // Step 1. Runs only when the row pointers passed their check (they index the
-// column array).
+// column array). Also keeps every block's block row for the later steps.
 __global__ void tiles_mark(Geom g, const int32_t* rowptr, const int32_t* colidx, const int32_t* bad,
-                           int32_t* maker, int32_t* is_maker, int32_t* bad_out) {
+                           int32_t* maker, int32_t* is_maker, int32_t* brow, int32_t* bad_out) {
   if (*bad & tiles::BAD_ROWPTR) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.nnzb; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = tiles::block_row_of(rowptr, g.nbr, i);
     int b = 0;
-    int64_t m = tiles::tile_maker(g, rowptr, colidx, i, &b);
+    int64_t m = tiles::tile_maker(g, rowptr, colidx, i, r, &b);
     if (b) {
       atomicOr(bad_out, b);
       m = i;
     }
     maker[i] = (int32_t)m;
     is_maker[i] = m == i ? 1 : 0;
+    brow[i] = (int32_t)r;
   }
 }
 
 // Step 3a: tile of every block; makers describe their tile.
-__global__ void tiles_place(Geom g, const int32_t* rowptr, const int32_t* colidx, const int32_t* maker,
+__global__ void tiles_place(Geom g, const int32_t* brow, const int32_t* colidx, const int32_t* maker,
                             const int32_t* tile_no, int32_t* tile_of_block, int32_t* tile_col, int32_t* tile_row,
                             int32_t* block_info) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.nnzb; i += (int64_t)gridDim.x * blockDim.x) {
@@ -159,8 +162,7 @@ __global__ void tiles_place(Geom g, const int32_t* rowptr, const int32_t* colidx
     const int32_t t = tile_no[m];
     tile_of_block[i] = t;
     if (m == i) {
-      const int64_t r = tiles::block_row_of(rowptr, g.nbr, i);
-      const int64_t x = colidx[i] / g.tw, y = r / 4;
+      const int64_t x = colidx[i] / g.tw, y = brow[i] / 4;
       tile_col[t] = (int32_t)(x * g.tw);
       tile_row[t] = (int32_t)y;
       block_info[y * g.tile_cols + x] = 1;
@@ -169,18 +171,34 @@ __global__ void tiles_place(Geom g, const int32_t* rowptr, const int32_t* colidx
 }
 
 // Step 3b: one warp per block copies its 16 x k values (32k bytes) into its
-// tile with 16-byte vectors.
-__global__ void tiles_scatter(Geom g, const int32_t* rowptr, const int32_t* colidx, const uint16_t* bval,
-                              const int32_t* tile_of_block, uint16_t* tval) {
+// tile with 16-byte vectors, and ORs the label flags of its rows into
+// positions (block row in tile, rho % 4) of the tile (tiles_core.h). A
+// lane's vectors all lie in rows with the same rho % 4.
+__global__ void tiles_scatter(Geom g, const int32_t* brow, const int32_t* colidx, const uint16_t* bval,
+                              const int32_t* tile_of_block, uint16_t* tval, int32_t* label_flags) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int nvec = 2 * g.k;  // 16-byte vectors per block
+  const int vpr = g.k / 8;   // 16-byte vectors per block row
+  const int nvec = 16 * vpr;  // 16-byte vectors per block
+  // lanes whose rows fall on position column sc = lane (lanes 0..3 use it)
+  uint32_t lanes_of_sc = 0;
+  for (int l = 0; l < 32; ++l) lanes_of_sc |= (((l / vpr) & 3) == (lane & 3) ? 1u : 0u) << l;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < g.nnzb; i += warps) {
-    const int64_t r = tiles::block_row_of(rowptr, g.nbr, i);
-    const int64_t off = (int64_t)tile_of_block[i] * g.tsz + tiles::block_offset_in_tile(g, r, colidx[i]);
+    const int64_t r = brow[i];
+    const int32_t t = tile_of_block[i];
+    const int64_t off = (int64_t)t * g.tsz + tiles::block_offset_in_tile(g, r, colidx[i]);
     const uint4* src = reinterpret_cast<const uint4*>(bval + i * 16 * g.k);
     uint4* dst = reinterpret_cast<uint4*>(tval + off);
-    for (int j = lane; j < nvec; j += 32) dst[j] = src[j];
+    int fl = 0;
+    for (int j = lane; j < nvec; j += 32) {
+      const uint4 v = src[j];
+      dst[j] = v;
+      fl |= tiles::group_flags(v.x, v.y) | tiles::group_flags(v.z, v.w);
+    }
+    const uint32_t any = __ballot_sync(0xffffffffu, fl & 1);
+    const uint32_t two = __ballot_sync(0xffffffffu, fl & 2);
+    if (lane < 4 && (any & lanes_of_sc))
+      atomicOr(&label_flags[(int64_t)t * 16 + 4 * (r % 4) + lane], (two & lanes_of_sc) ? 3 : 1);
   }
 }
 
@@ -205,10 +223,10 @@ __global__ void tiles_rel_fix(int64_t cells, const int32_t* block_info, int32_t*
     if (!block_info[c]) rel_map[c] = -1;
 }
 
-// Step 4d: the 16 labels of every tile.
-__global__ void tiles_labels(Geom g, int64_t nt, const uint16_t* tval, int32_t* tile_info) {
+// Step 4d: label flags -> the 16 labels of every tile, in place.
+__global__ void tiles_labels(int64_t nt, int32_t* tile_info) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nt * 16; e += (int64_t)gridDim.x * blockDim.x)
-    tile_info[e] = tiles::tile_label(g, tval + (e / 16) * g.tsz, (int)(e % 16));
+    tile_info[e] = tiles::label_of_flags(tile_info[e]);
 }
 
 }  // namespace dev
@@ -315,7 +333,7 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
   TILES_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, res->device), "device attribute");
 
   // counters: [0] input faults, [1] tiles, [2] tile rows with a tile, [3] grid total
-  DevBuf cnt, maker, is_maker, tile_no, chunks;
+  DevBuf cnt, maker, is_maker, tile_no, brow, chunks;
   TILES_CUDA(cnt.alloc(4 * sizeof(int32_t)), "scratch");
   TILES_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * sizeof(int32_t), s), "memset");
   const int64_t scan_max = nnzb > cells ? nnzb : cells;
@@ -324,6 +342,7 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
   TILES_CUDA(maker.alloc(sizeof(int32_t) * (size_t)nnzb), "scratch");
   TILES_CUDA(is_maker.alloc(sizeof(int32_t) * (size_t)nnzb), "scratch");
   TILES_CUDA(tile_no.alloc(sizeof(int32_t) * (size_t)nnzb), "scratch");
+  TILES_CUDA(brow.alloc(sizeof(int32_t) * (size_t)nnzb), "scratch");
   int32_t* c = cnt.as<int32_t>();
 
   // steps 1-2
@@ -333,7 +352,7 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
   }
   if (nnzb > 0) {
     dev::tiles_mark<<<grid_for(nnzb, sms), 256, 0, s>>>(g, row_ptr, col_idx, c, maker.as<int32_t>(),
-                                                         is_maker.as<int32_t>(), c);
+                                                         is_maker.as<int32_t>(), brow.as<int32_t>(), c);
     TILES_CUDA(cudaGetLastError(), "launch");
   }
   TILES_CUDA(exclusive_scan(is_maker.as<int32_t>(), nnzb, tile_no.as<int32_t>(), chunks.as<int32_t>(), c + 1, s),
@@ -359,6 +378,7 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
   TILES_CUDA(cudaMemsetAsync(res->val, 0, sizeof(uint16_t) * (size_t)(nt * g.tsz), s), "memset");
   TILES_CUDA(cudaMemsetAsync(res->rowptr, 0, sizeof(int32_t) * (size_t)(max_rows_used + 1), s), "memset");
   TILES_CUDA(cudaMemsetAsync(res->block_info, 0, sizeof(int32_t) * (size_t)cells, s), "memset");
+  TILES_CUDA(cudaMemsetAsync(res->tile_info, 0, sizeof(int32_t) * (size_t)(nt * 16), s), "memset");
 
   // steps 3-4
   DevBuf tile_of_block, tile_row, start, rank;
@@ -367,12 +387,13 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
   TILES_CUDA(start.alloc(sizeof(int32_t) * (size_t)nt), "scratch");
   TILES_CUDA(rank.alloc(sizeof(int32_t) * (size_t)nt), "scratch");
   if (nnzb > 0) {
-    dev::tiles_place<<<grid_for(nnzb, sms), 256, 0, s>>>(g, row_ptr, col_idx, maker.as<int32_t>(),
+    dev::tiles_place<<<grid_for(nnzb, sms), 256, 0, s>>>(g, brow.as<int32_t>(), col_idx, maker.as<int32_t>(),
                                                           tile_no.as<int32_t>(), tile_of_block.as<int32_t>(),
                                                           res->colidx, tile_row.as<int32_t>(), res->block_info);
-    dev::tiles_scatter<<<grid_for(nnzb * 32, sms), 256, 0, s>>>(g, row_ptr, col_idx,
+    dev::tiles_scatter<<<grid_for(nnzb * 32, sms), 256, 0, s>>>(g, brow.as<int32_t>(), col_idx,
                                                                  static_cast<const uint16_t*>(values),
-                                                                 tile_of_block.as<int32_t>(), res->val);
+                                                                 tile_of_block.as<int32_t>(), res->val,
+                                                                 res->tile_info);
     dev::tiles_row_starts<<<grid_for(nt, sms), 256, 0, s>>>(nt, tile_row.as<int32_t>(), start.as<int32_t>());
     TILES_CUDA(cudaGetLastError(), "launch");
   }
@@ -388,7 +409,7 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
     TILES_CUDA(cudaGetLastError(), "launch");
   }
   if (nt > 0) {
-    dev::tiles_labels<<<grid_for(nt * 16, sms), 256, 0, s>>>(g, nt, res->val, res->tile_info);
+    dev::tiles_labels<<<grid_for(nt * 16, sms), 256, 0, s>>>(nt, res->tile_info);
     TILES_CUDA(cudaGetLastError(), "launch");
   }
   TILES_CUDA(cudaMemcpyAsync(hc, c, sizeof(hc), cudaMemcpyDeviceToHost, s), "copy");

@@ -97,12 +97,12 @@ SMAT_TILES_HD int check_row(const Geom& g, const int32_t* rowptr, int64_t r) {
   return bad;
 }
 
-// Step 1, block i (row pointers already checked): the index of the block
-// that made i's tile (i itself when i makes it), or -1 with *bad set when
-// i's column start is out of range, not a multiple of k, or not above the
-// previous block's in the same block row.
-SMAT_TILES_HD int64_t tile_maker(const Geom& g, const int32_t* rowptr, const int32_t* colidx, int64_t i, int* bad) {
-  const int64_t r = block_row_of(rowptr, g.nbr, i);
+// Step 1, block i in block row r (row pointers already checked): the index
+// of the block that made i's tile (i itself when i makes it), or -1 with
+// *bad set when i's column start is out of range, not a multiple of k, or
+// not above the previous block's in the same block row.
+SMAT_TILES_HD int64_t tile_maker(const Geom& g, const int32_t* rowptr, const int32_t* colidx, int64_t i, int64_t r,
+                                 int* bad) {
   const int64_t col = colidx[i];
   if (col < 0 || col >= g.m_col || col % g.k != 0) {
     *bad |= BAD_COLIDX;
@@ -128,11 +128,41 @@ SMAT_TILES_HD int64_t block_offset_in_tile(const Geom& g, int64_t r, int64_t col
   return 16 * (int64_t)g.k * (4 * by + bx);
 }
 
-// Step 4: the label of position s (0..15) of a tile, read the way the
-// reference reads it (matrix.h:1036-1088): the tile's values taken as a
-// ROW-MAJOR 64 x 4k matrix, rows 16 (s / 4) .. +15, columns k (s % 4) .. +k-1;
-// 0: all zero, 1: no group of four with more than two nonzeros, 2: otherwise.
-// A value is nonzero unless it is +0 or -0.
+// Labels. The reference labels position s (0..15) of a tile by reading the
+// tile's values as a ROW-MAJOR 64 x 4k matrix, rows 16 (s / 4) .. +15,
+// columns k (s % 4) .. +k-1 (matrix.h:1036-1088): 0 all zero, 1 no group of
+// four with more than two nonzeros, 2 otherwise (a value is nonzero unless
+// it is +0 or -0). The tile stores its blocks block-major, so row R of that
+// view is the 4k values of rows 4 (R % 4) .. +3 of block R / 4, and columns
+// k (s % 4) .. +k-1 of it are row 4 (R % 4) + s % 4 of that block: position
+// (sr, sc) looks at the rows rho with rho % 4 == sc of the four blocks of the
+// tile's block row sr. So each block can add its share while it is copied:
+// flags per sc (bit 0: a nonzero, bit 1: a group of four with more than two),
+// ORed into the position and turned into the label at the end.
+
+// Flags of one group of four FP16 values given as two 32-bit words.
+SMAT_TILES_HD int group_flags(uint32_t lo, uint32_t hi) {
+  const int nz = ((lo & 0x7fffu) != 0) + ((lo & 0x7fff0000u) != 0) + ((hi & 0x7fffu) != 0) +
+                 ((hi & 0x7fff0000u) != 0);
+  return (nz > 0 ? 1 : 0) | (nz > 2 ? 2 : 0);
+}
+
+// Flags a block (16 x k values, row-major) adds to positions (by, 0..3) of
+// its tile: flags[sc] from its rows rho with rho % 4 == sc.
+SMAT_TILES_HD void block_label_flags(const Geom& g, const uint16_t* blk, int flags[4]) {
+  for (int sc = 0; sc < 4; ++sc) flags[sc] = 0;
+  for (int rho = 0; rho < 16; ++rho)
+    for (int c = 0; c < g.k; c += 4) {
+      const uint16_t* q = blk + rho * g.k + c;
+      flags[rho % 4] |= group_flags((uint32_t)q[0] | ((uint32_t)q[1] << 16), (uint32_t)q[2] | ((uint32_t)q[3] << 16));
+    }
+}
+
+// Label from the ORed flags of a position.
+SMAT_TILES_HD int32_t label_of_flags(int v) { return (v & 2) ? 2 : (v & 1); }
+
+// The label of position s read directly from a whole tile, as the reference
+// reads it (the CPU replay checks the block-wise flags against it).
 SMAT_TILES_HD int32_t tile_label(const Geom& g, const uint16_t* tile, int s) {
   const int sr = s / 4, sc = s % 4;
   bool any = false, two_four = true;
