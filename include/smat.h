@@ -246,9 +246,10 @@ smat_status smat_csr_to_bcsr_split_host(const smat_csr* A, int32_t block_cols, c
  *   tile_info  [n_tiles * 16]: the reference's 0 / 1 / 2 labels, computed as
  *              it computes them (the tile read as a row-major 64 x 4k matrix)
  * with tile_rows = ceil(rows/64), tile_cols = ceil(cols/(4*block_cols)).
- * Runs on `stream` and synchronises it (the tile count sizes the outputs);
- * allocates its outputs and scratch on the current device. Invalid row
- * pointers or column starts give SMAT_ERR_INVALID. */
+ * The three input arrays are device (or managed) memory of the current
+ * device. Runs on `stream` and synchronises it (the tile count sizes the
+ * outputs); allocates its outputs and scratch on the current device.
+ * Invalid row pointers or column starts give SMAT_ERR_INVALID. */
 typedef struct smat_tiles smat_tiles; /* opaque, owns the device arrays */
 typedef struct smat_tiles_desc {
   int64_t rows, cols;

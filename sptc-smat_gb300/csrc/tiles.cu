@@ -329,6 +329,20 @@ extern "C" smat_status smat_tiles_create(int64_t rows, int64_t cols, int32_t blo
   smat_tiles* res = new smat_tiles;
   res->g = g;
   TILES_CUDA(cudaGetDevice(&res->device), "cudaGetDevice");
+  // the kernels dereference the three arrays: they must be device (or
+  // managed) memory of the current device
+  for (const void* p : {static_cast<const void*>(row_ptr), static_cast<const void*>(col_idx), values}) {
+    if (!p) continue;
+    cudaPointerAttributes pa{};
+    const cudaError_t e = cudaPointerGetAttributes(&pa, p);
+    if (e != cudaSuccess || !(pa.type == cudaMemoryTypeManaged ||
+                              (pa.type == cudaMemoryTypeDevice && pa.device == res->device))) {
+      cudaGetLastError();
+      free_tiles(res);
+      return fail(SMAT_ERR_INVALID, "smat_tiles_create: row_ptr, col_idx and values must be device memory of "
+                                    "the current device");
+    }
+  }
   int sms = 0;
   TILES_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, res->device), "device attribute");
 
